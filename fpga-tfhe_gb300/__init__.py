@@ -1,0 +1,365 @@
+"""Host-side binding of the GB300 TFHE engine (ctypes over include/tfhe_gpu.h).
+
+This mirrors the reference's operator interface for the bootstrapping path
+(kernel/src/include/fpga_constants.h:57-69, the upstream gate calls of
+test_bench/server/cloud.c:10-35): one method per C entry point, same names,
+device-batch forms over device buffers (any object with a data_ptr(), e.g.
+torch tensors, or raw integer addresses) and host-buffer forms over numpy
+arrays.  Errors raise TfheError carrying the status and the context's
+last_error; there is no CPU fallback -- if the shared library is missing the
+import fails loudly.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libtfhe_gb300.so")
+
+I32P = ctypes.POINTER(ctypes.c_int32)
+U32P = ctypes.POINTER(ctypes.c_uint32)
+F64P = ctypes.POINTER(ctypes.c_double)
+VP = ctypes.c_void_p
+
+FP64 = 0
+SPLIT_FP32 = 1
+FORMS = {"fp64": FP64, "split_fp32": SPLIT_FP32}
+
+GATES = {"NAND": 0, "AND": 1, "OR": 2, "XOR": 3, "XNOR": 4, "NOR": 5,
+         "ANDNY": 6, "ANDYN": 7, "ORNY": 8, "ORYN": 9}
+
+STATUS = {0: "ok", 1: "bad parameter", 2: "out of memory", 3: "timeout",
+          4: "device error", 5: "key not uploaded"}
+
+
+class TfheError(RuntimeError):
+    def __init__(self, status, detail):
+        super().__init__("%s (%d): %s" % (STATUS.get(status, "?"), status, detail))
+        self.status = status
+
+
+class Params(ctypes.Structure):
+    """tfhe_params (include/tfhe_gpu.h)."""
+    _fields_ = [("n", ctypes.c_int32), ("N", ctypes.c_int32), ("k", ctypes.c_int32),
+                ("l", ctypes.c_int32), ("Bgbit", ctypes.c_int32), ("ks_t", ctypes.c_int32),
+                ("ks_basebit", ctypes.c_int32), ("split_bits", ctypes.c_int32),
+                ("lwe_alpha", ctypes.c_double), ("tlwe_alpha", ctypes.c_double)]
+
+    @property
+    def kpl(self):
+        return (self.k + 1) * self.l
+
+    def tgsw_words(self):
+        return self.kpl * (self.k + 1) * self.N
+
+    def ks_words(self):
+        return self.k * self.N * self.ks_t * (1 << self.ks_basebit) * (self.n + 1)
+
+
+def default_params():
+    """The reference's default gate set (constants.h:26-40)."""
+    return Params(n=630, N=1024, k=1, l=3, Bgbit=7, ks_t=8, ks_basebit=2, split_bits=0,
+                  lwe_alpha=2.0 ** -15, tlwe_alpha=2.0 ** -25)
+
+
+def stress_params():
+    """Alternative set: n=500, l=2, Bgbit=10, LWE 2^-15, TRLWE 2^-24."""
+    return Params(n=500, N=1024, k=1, l=2, Bgbit=10, ks_t=8, ks_basebit=2, split_bits=0,
+                  lwe_alpha=2.0 ** -15, tlwe_alpha=2.0 ** -24)
+
+
+# Every symbol of include/tfhe_gpu.h with its ctypes signature.
+SIGNATURES = {
+    "tfhe_gpu_default_params": (None, [ctypes.c_void_p]),
+    "tfhe_gpu_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(VP)]),
+    "tfhe_gpu_destroy": (None, [VP]),
+    "tfhe_gpu_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "tfhe_gpu_last_error": (ctypes.c_char_p, [VP]),
+    "tfhe_gpu_get_params": (ctypes.c_int, [VP, ctypes.c_void_p]),
+    "tfhe_gpu_stream": (VP, [VP]),
+    "tfhe_gpu_synchronize": (ctypes.c_int, [VP]),
+    "tfhe_gpu_tgsw_fft_bytes": (ctypes.c_size_t, [VP, ctypes.c_int]),
+    "tfhe_gpu_device_bytes": (ctypes.c_size_t, [VP]),
+    "tfhe_gpu_upload_bootstrapping_key": (ctypes.c_int, [VP, I32P, ctypes.c_uint32]),
+    "tfhe_gpu_upload_bootstrapping_key_fft": (ctypes.c_int, [VP, F64P, ctypes.c_uint32]),
+    "tfhe_gpu_upload_keyswitch_key": (ctypes.c_int, [VP, I32P]),
+    "tfhe_gpu_tgsw_to_fft": (ctypes.c_int, [VP, VP, VP, ctypes.c_int32, ctypes.c_int, VP]),
+    "tfhe_gpu_IntPolynomial_ifft": (ctypes.c_int, [VP, VP, VP, ctypes.c_int32, VP]),
+    "tfhe_gpu_TorusPolynomial_ifft": (ctypes.c_int, [VP, VP, VP, ctypes.c_int32, VP]),
+    "tfhe_gpu_TorusPolynomial_fft": (ctypes.c_int, [VP, VP, VP, ctypes.c_int32, VP]),
+    "tfhe_gpu_LagrangeHalfCPolynomialAddMul": (ctypes.c_int, [VP, VP, VP, VP, ctypes.c_int32, VP]),
+    "tfhe_gpu_tLweMulByXaiMinusOne": (ctypes.c_int, [VP, VP, VP, VP, ctypes.c_int32, VP]),
+    "tfhe_gpu_tGswFFTExternMulToTLwe": (ctypes.c_int, [VP, VP, VP, ctypes.c_int32, ctypes.c_int32,
+                                                       ctypes.c_int, VP]),
+    "tfhe_gpu_tfhe_MuxRotate_FFT": (ctypes.c_int, [VP, VP, VP, VP, ctypes.c_int32, VP,
+                                                   ctypes.c_int32, ctypes.c_int, VP]),
+    "tfhe_gpu_tfhe_blindRotate_FFT": (ctypes.c_int, [VP, VP, VP, ctypes.c_int32, ctypes.c_int, VP]),
+    "tfhe_gpu_tLweExtractLweSample": (ctypes.c_int, [VP, VP, VP, ctypes.c_int32, VP]),
+    "tfhe_gpu_lweKeySwitch": (ctypes.c_int, [VP, VP, VP, ctypes.c_int32, VP]),
+    "tfhe_gpu_tfhe_bootstrap_woKS_FFT": (ctypes.c_int, [VP, VP, VP, ctypes.c_int32, ctypes.c_int32,
+                                                        ctypes.c_int, VP]),
+    "tfhe_gpu_tfhe_bootstrap_FFT": (ctypes.c_int, [VP, VP, VP, ctypes.c_int32, ctypes.c_int32,
+                                                   ctypes.c_int, VP]),
+    "tfhe_gpu_bootsGate": (ctypes.c_int, [VP, ctypes.c_int32, VP, VP, VP, ctypes.c_int32,
+                                          ctypes.c_int, VP]),
+    "tfhe_gpu_bootsGates": (ctypes.c_int, [VP, VP, VP, VP, VP, ctypes.c_int32, ctypes.c_int, VP]),
+    "tfhe_gpu_bootsMUX": (ctypes.c_int, [VP, VP, VP, VP, VP, ctypes.c_int32, ctypes.c_int, VP]),
+    "tfhe_gpu_bootsGates_host": (ctypes.c_int, [VP, I32P, ctypes.c_int32, I32P, I32P, I32P,
+                                                ctypes.c_int32, ctypes.c_int]),
+    "tfhe_client_set_seed": (None, [U32P, ctypes.c_int32]),
+    "tfhe_client_gate_keyset": (ctypes.c_int, [ctypes.c_void_p, I32P, I32P, I32P, I32P]),
+    "tfhe_client_encrypt_bits": (ctypes.c_int, [ctypes.c_void_p, I32P, ctypes.c_int32, I32P, I32P]),
+    "tfhe_client_decrypt_bits": (ctypes.c_int, [ctypes.c_void_p, I32P, ctypes.c_int32, I32P, I32P]),
+    "tfhe_client_phases": (None, [I32P, ctypes.c_int32, ctypes.c_int32, I32P, I32P]),
+    "tfhe_client_mod_switch_to_torus32": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32]),
+}
+
+_LIB = None
+
+
+def lib():
+    """Load the engine's shared library (fails loudly if it was not built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libtfhe_gb300.so not built: run __graft_entry__.build() "
+                              "(nvcc, sm_103a); there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _np(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def _ptr(x):
+    """Device address of a tensor-like object, a raw int, or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+# ---- client side (host only) -------------------------------------------------
+
+def set_seed(values):
+    v = _np(values, np.uint32)
+    lib().tfhe_client_set_seed(v.ctypes.data_as(U32P), len(v))
+
+
+def gate_keyset(P, seed):
+    """Seed the generator and produce (lwe_key, tlwe_key, ks, bk) like the
+    upstream new_random_gate_bootstrapping_secret_keyset."""
+    set_seed(seed)
+    lwe = np.zeros(P.n, np.int32)
+    tlwe = np.zeros(P.k * P.N, np.int32)
+    ks = np.zeros(P.ks_words(), np.int32)
+    bk = np.zeros(P.n * P.tgsw_words(), np.int32)
+    st = lib().tfhe_client_gate_keyset(ctypes.byref(P), lwe.ctypes.data_as(I32P),
+                                       tlwe.ctypes.data_as(I32P), ks.ctypes.data_as(I32P),
+                                       bk.ctypes.data_as(I32P))
+    if st:
+        raise TfheError(st, "gate_keyset")
+    return lwe, tlwe, ks, bk
+
+
+def encrypt_bits(P, bits, lwe_key):
+    bits = _np(bits, np.int32)
+    out = np.zeros((len(bits), P.n + 1), np.int32)
+    st = lib().tfhe_client_encrypt_bits(ctypes.byref(P), bits.ctypes.data_as(I32P), len(bits),
+                                        _np(lwe_key, np.int32).ctypes.data_as(I32P),
+                                        out.ctypes.data_as(I32P))
+    if st:
+        raise TfheError(st, "encrypt_bits")
+    return out
+
+
+def decrypt_bits(P, samples, lwe_key):
+    s = _np(samples, np.int32).reshape(-1, P.n + 1)
+    out = np.zeros(len(s), np.int32)
+    st = lib().tfhe_client_decrypt_bits(ctypes.byref(P), s.ctypes.data_as(I32P), len(s),
+                                        _np(lwe_key, np.int32).ctypes.data_as(I32P),
+                                        out.ctypes.data_as(I32P))
+    if st:
+        raise TfheError(st, "decrypt_bits")
+    return out
+
+
+def phases(samples, key):
+    key = _np(key, np.int32)
+    dim = len(key)
+    s = _np(samples, np.int32).reshape(-1, dim + 1)
+    out = np.zeros(len(s), np.int32)
+    lib().tfhe_client_phases(s.ctypes.data_as(I32P), len(s), dim, key.ctypes.data_as(I32P),
+                             out.ctypes.data_as(I32P))
+    return out
+
+
+# ---- engine ------------------------------------------------------------------
+
+class Engine:
+    """One engine context on one device (tfhe_gpu_ctx)."""
+
+    def __init__(self, params=None, device=0):
+        self.lib = lib()
+        if params is None:
+            params = default_params()
+        h = VP()
+        st = self.lib.tfhe_gpu_create(ctypes.byref(params), int(device), ctypes.byref(h))
+        if st:
+            raise TfheError(st, "tfhe_gpu_create")
+        self.ctx = h
+        self.params = Params()
+        self.lib.tfhe_gpu_get_params(self.ctx, ctypes.byref(self.params))
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.tfhe_gpu_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st:
+            raise TfheError(st, "%s: %s" % (what, self.lib.tfhe_gpu_last_error(self.ctx).decode()))
+
+    @staticmethod
+    def _form(form):
+        return FORMS[form] if isinstance(form, str) else int(form)
+
+    @property
+    def stream(self):
+        return self.lib.tfhe_gpu_stream(self.ctx)
+
+    def synchronize(self):
+        self._check(self.lib.tfhe_gpu_synchronize(self.ctx), "synchronize")
+
+    def tgsw_fft_bytes(self, form):
+        return self.lib.tfhe_gpu_tgsw_fft_bytes(self.ctx, self._form(form))
+
+    def device_bytes(self):
+        return self.lib.tfhe_gpu_device_bytes(self.ctx)
+
+    # keys
+    def upload_bootstrapping_key(self, bk, forms=("fp64", "split_fp32")):
+        mask = 0
+        for f in forms:
+            mask |= 1 << self._form(f)
+        bk = _np(bk, np.int32)
+        self._check(self.lib.tfhe_gpu_upload_bootstrapping_key(self.ctx, bk.ctypes.data_as(I32P), mask),
+                    "upload_bootstrapping_key")
+
+    def upload_bootstrapping_key_fft(self, bk_fft, forms=("fp64", "split_fp32")):
+        mask = 0
+        for f in forms:
+            mask |= 1 << self._form(f)
+        bk_fft = _np(bk_fft, np.float64)
+        self._check(self.lib.tfhe_gpu_upload_bootstrapping_key_fft(
+            self.ctx, bk_fft.ctypes.data_as(F64P), mask), "upload_bootstrapping_key_fft")
+
+    def upload_keyswitch_key(self, ks):
+        ks = _np(ks, np.int32)
+        self._check(self.lib.tfhe_gpu_upload_keyswitch_key(self.ctx, ks.ctypes.data_as(I32P)),
+                    "upload_keyswitch_key")
+
+    # device-batch entry points (arguments: device buffers)
+    def tgsw_to_fft(self, tgsw, out, count, form, stream=None):
+        self._check(self.lib.tfhe_gpu_tgsw_to_fft(self.ctx, _ptr(tgsw), _ptr(out), count,
+                                                  self._form(form), stream), "tgsw_to_fft")
+
+    def IntPolynomial_ifft(self, polys, out, count, stream=None):
+        self._check(self.lib.tfhe_gpu_IntPolynomial_ifft(self.ctx, _ptr(polys), _ptr(out), count, stream),
+                    "IntPolynomial_ifft")
+
+    def TorusPolynomial_ifft(self, polys, out, count, stream=None):
+        self._check(self.lib.tfhe_gpu_TorusPolynomial_ifft(self.ctx, _ptr(polys), _ptr(out), count,
+                                                           stream), "TorusPolynomial_ifft")
+
+    def TorusPolynomial_fft(self, values, polys, count, stream=None):
+        self._check(self.lib.tfhe_gpu_TorusPolynomial_fft(self.ctx, _ptr(values), _ptr(polys), count,
+                                                          stream), "TorusPolynomial_fft")
+
+    def LagrangeHalfCPolynomialAddMul(self, accum, a, b, count, stream=None):
+        self._check(self.lib.tfhe_gpu_LagrangeHalfCPolynomialAddMul(self.ctx, _ptr(accum), _ptr(a), _ptr(b),
+                                                                    count, stream),
+                    "LagrangeHalfCPolynomialAddMul")
+
+    def tLweMulByXaiMinusOne(self, out, ai, inp, count, stream=None):
+        self._check(self.lib.tfhe_gpu_tLweMulByXaiMinusOne(self.ctx, _ptr(out), _ptr(ai), _ptr(inp), count,
+                                                           stream), "tLweMulByXaiMinusOne")
+
+    def tGswFFTExternMulToTLwe(self, accum, gsw, count, form, per_item=True, stream=None):
+        self._check(self.lib.tfhe_gpu_tGswFFTExternMulToTLwe(self.ctx, _ptr(accum), _ptr(gsw),
+                                                             1 if per_item else 0, count,
+                                                             self._form(form), stream),
+                    "tGswFFTExternMulToTLwe")
+
+    def tfhe_MuxRotate_FFT(self, result, accum, gsw, barai, count, form, per_item=True, stream=None):
+        self._check(self.lib.tfhe_gpu_tfhe_MuxRotate_FFT(self.ctx, _ptr(result), _ptr(accum), _ptr(gsw),
+                                                         1 if per_item else 0, _ptr(barai), count,
+                                                         self._form(form), stream),
+                    "tfhe_MuxRotate_FFT")
+
+    def tfhe_blindRotate_FFT(self, accum, bara, count, form, stream=None):
+        self._check(self.lib.tfhe_gpu_tfhe_blindRotate_FFT(self.ctx, _ptr(accum), _ptr(bara), count,
+                                                           self._form(form), stream),
+                    "tfhe_blindRotate_FFT")
+
+    def tLweExtractLweSample(self, out, accum, count, stream=None):
+        self._check(self.lib.tfhe_gpu_tLweExtractLweSample(self.ctx, _ptr(out), _ptr(accum), count,
+                                                           stream), "tLweExtractLweSample")
+
+    def lweKeySwitch(self, out, inp, count, stream=None):
+        self._check(self.lib.tfhe_gpu_lweKeySwitch(self.ctx, _ptr(out), _ptr(inp), count, stream),
+                    "lweKeySwitch")
+
+    def tfhe_bootstrap_woKS_FFT(self, out, x, mu, count, form, stream=None):
+        self._check(self.lib.tfhe_gpu_tfhe_bootstrap_woKS_FFT(self.ctx, _ptr(out), _ptr(x), int(mu),
+                                                              count, self._form(form), stream),
+                    "tfhe_bootstrap_woKS_FFT")
+
+    def tfhe_bootstrap_FFT(self, out, x, mu, count, form, stream=None):
+        self._check(self.lib.tfhe_gpu_tfhe_bootstrap_FFT(self.ctx, _ptr(out), _ptr(x), int(mu), count,
+                                                         self._form(form), stream),
+                    "tfhe_bootstrap_FFT")
+
+    def bootsGate(self, gate, out, ca, cb, count, form, stream=None):
+        g = GATES[gate] if isinstance(gate, str) else int(gate)
+        self._check(self.lib.tfhe_gpu_bootsGate(self.ctx, g, _ptr(out), _ptr(ca), _ptr(cb), count,
+                                                self._form(form), stream), "bootsGate")
+
+    def bootsGates(self, gates, out, ca, cb, count, form, stream=None):
+        self._check(self.lib.tfhe_gpu_bootsGates(self.ctx, _ptr(gates), _ptr(out), _ptr(ca), _ptr(cb),
+                                                 count, self._form(form), stream), "bootsGates")
+
+    def bootsMUX(self, out, a, b, c, count, form, stream=None):
+        self._check(self.lib.tfhe_gpu_bootsMUX(self.ctx, _ptr(out), _ptr(a), _ptr(b), _ptr(c), count,
+                                               self._form(form), stream), "bootsMUX")
+
+    # host-buffer form (end to end)
+    def bootsGates_host(self, ca, cb, gates=None, gate="NAND", form="split_fp32", out=None):
+        ca = _np(ca, np.int32)
+        cb = _np(cb, np.int32)
+        count = ca.shape[0]
+        if out is None:
+            out = np.zeros_like(ca)
+        gp = None
+        if gates is not None:
+            gates = _np(gates, np.int32)
+            gp = gates.ctypes.data_as(I32P)
+        g = GATES[gate] if isinstance(gate, str) else int(gate)
+        self._check(self.lib.tfhe_gpu_bootsGates_host(self.ctx, gp, g, out.ctypes.data_as(I32P),
+                                                      ca.ctypes.data_as(I32P), cb.ctypes.data_as(I32P),
+                                                      count, self._form(form)), "bootsGates_host")
+        return out

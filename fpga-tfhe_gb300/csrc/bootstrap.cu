@@ -1,0 +1,808 @@
+// bootstrap.cu -- FFT-domain kernels of the GB300 TFHE engine:
+//   * key conversion (TGSW time domain -> engine FFT layout, both forms)
+//   * the external product, MuxRotate and the blind-rotation loop, one
+//     kernel template (EpMode) built on a fused step:
+//       rotate (X^a - 1) -> gadget digits -> twisted FFT-512 -> MAC against
+//       the key -> inverse FFT-512 -> Torus32 -> accumulate
+//   * bootstrap front end (modulus switch, rotated test vector) and sample
+//     extraction, fused into the blind-rotation kernel
+//   * small kernels: gate combination, X^a - 1 rotation, extraction
+//   * the Lagrange processor (polynomial <-> Lagrange half-complex form in
+//     the reference's layout)
+//
+// Reference call stack restated here (paths inside shreks99/fpga-tfhe):
+//   tfhe_blindRotate_FFT         kernel/src/tfhe_blindRotate_FFT/tfhe_blindRotate_FFT.cpp:61-147
+//   tfhe_MuxRotate_FFT_FPGA      .../tfhe_MuxRotate_FFT.cpp:56-85
+//   tLweMulByXaiMinusOne_FPGA    .../tfhe_MuxRotate_FFT.cpp:5-33
+//   tGswFFTExternMulToTLwe_FPGA  .../tGswFFTExternMulToTLwe.cpp:203-247
+//   decompose                    .../tGswFFTExternMulToTLwe.cpp:76-95
+//   ifft (Int -> Lagrange)       .../tGswFFTExternMulToTLwe.cpp:97-130
+//   MAC                          .../tGswFFTExternMulToTLwe.cpp:166-197
+//   TorusPolynomial_fft          .../TorusPolynomial_fft.cpp:4-43
+//   modulus switch / test vector kernel/src/tfhe_bootstrap_woKS_FFT/tfhe_bootstrap_woKS_FFT.cpp:3-10,57-66
+//   X^{2N-b} rotation            kernel/src/tfhe_blindRotateAndExtract/mulByXaiOrCopy.cpp:25-41
+#include <math.h>
+
+#include "engine.h"
+#include "fft512.cuh"
+
+namespace tfhe_gb300 {
+
+namespace {
+
+constexpr int kN = 1024;
+constexpr int kHalf = 512;
+
+// ----------------------------------------------------------------------
+// helpers
+// ----------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ const cpx<R>* table_ptr(const Tables& T);
+template <>
+__device__ __forceinline__ const cpx<float>* table_ptr<float>(const Tables& T) {
+    return reinterpret_cast<const cpx<float>*>(T.tw32);
+}
+template <>
+__device__ __forceinline__ const cpx<double>* table_ptr<double>(const Tables& T) {
+    return reinterpret_cast<const cpx<double>*>(T.tw64);
+}
+
+__device__ __forceinline__ int32_t mod_switch_2n(int32_t phase) {
+    // numeric-functions.cpp:59-65 with Msize = 2N = 2048
+    const uint64_t interv = ((UINT64_C(1) << 63) / 2048u) * 2;
+    const uint64_t half_interval = interv / 2;
+    const uint64_t phase64 = ((uint64_t)(int64_t)phase << 32) + half_interval;
+    return (int32_t)(phase64 / interv);
+}
+
+// (X^a * p)[x] for a in [0, 2N): s = (x - a) mod 2N; +p[s] or -p[s - N].
+__device__ __forceinline__ int32_t rot_coef(const int32_t* p, int x, int a) {
+    const int s = (x - a) & (2 * kN - 1);
+    const int32_t v = p[s & (kN - 1)];
+    return s < kN ? v : (int32_t)(0u - (uint32_t)v);
+}
+
+template <typename R>
+__device__ __forceinline__ int64_t to_int(R v);
+template <>
+__device__ __forceinline__ int64_t to_int<double>(double v) {
+    // reference semantics: int64_t(double) truncates (TorusPolynomial_fft.cpp:40)
+    return __double2ll_rz(v);
+}
+template <>
+__device__ __forceinline__ int64_t to_int<float>(float v) {
+    return __float2ll_rn(v);
+}
+
+// ----------------------------------------------------------------------
+// shared-memory plan of the FFT kernels
+//   [tables: 1024 cpx<R>] then per 64-thread group:
+//   [acc: 2 x 1024 int32][scratch: 4 x 576 R]
+// ----------------------------------------------------------------------
+template <typename R>
+struct SmemPlan {
+    static constexpr size_t tables = 1024 * sizeof(cpx<R>);
+    static constexpr size_t acc = 2 * kN * sizeof(int32_t);
+    static constexpr size_t scratch = 4 * kScratchStride * sizeof(R);
+    static constexpr size_t group = acc + scratch;
+    static size_t total(int groups) { return tables + groups * group; }
+};
+
+template <typename R>
+__device__ __forceinline__ FftScratch<R> scratch_at(char* base) {
+    R* s = reinterpret_cast<R*>(base);
+    return {s, s + kScratchStride, s + 2 * kScratchStride, s + 3 * kScratchStride};
+}
+
+template <typename R>
+__device__ __forceinline__ void load_tables(cpx<R>* dst, const Tables& T) {
+    const cpx<R>* src = table_ptr<R>(T);
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) dst[i] = src[i];
+}
+
+// ----------------------------------------------------------------------
+// the fused step: out = EP(ROT ? (X^a - 1) acc : acc);
+//                 acc = (ROT ? acc : 0) + out
+// gsw: one TGSW in engine layout [kpl][2][PARTS][512 key_index order].
+// ----------------------------------------------------------------------
+template <typename R, int PARTS>
+struct StepCtx {
+    const cpx<R>* tw;   // smem W_512^k
+    const cpx<R>* psi;  // smem psi^x
+    FftScratch<R> s;
+    int32_t* acc;       // smem 2 x N
+    int t, bar_id;
+    int l, Bgbit, split;
+    uint32_t offset;
+};
+
+template <typename R, int PARTS, bool ROT>
+__device__ __forceinline__ void ep_step(const StepCtx<R, PARTS>& S,
+                                        const cpx<R>* __restrict__ gsw, int a) {
+    const int t = S.t;
+    const int halfBg = 1 << (S.Bgbit - 1);
+    const uint32_t mask = (1u << S.Bgbit) - 1;
+
+    cpx<R> out[2][PARTS][8];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int pt = 0; pt < PARTS; ++pt)
+#pragma unroll
+            for (int q = 0; q < 8; ++q) out[j][pt][q] = {(R)0, (R)0};
+
+    for (int jp = 0; jp < 2; ++jp) {
+        const int32_t* src = S.acc + jp * kN;
+        uint32_t r0[8], r1[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int x0 = t + 64 * r;
+            if (ROT) {
+                r0[r] = (uint32_t)rot_coef(src, x0, a) - (uint32_t)src[x0];
+                r1[r] = (uint32_t)rot_coef(src, x0 + kHalf, a) - (uint32_t)src[x0 + kHalf];
+            } else {
+                r0[r] = (uint32_t)src[x0];
+                r1[r] = (uint32_t)src[x0 + kHalf];
+            }
+            r0[r] += S.offset;
+            r1[r] += S.offset;
+        }
+        for (int lev = 0; lev < S.l; ++lev) {
+            const int p = jp * S.l + lev;
+            const int decal = 32 - (lev + 1) * S.Bgbit;
+            cpx<R> v[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int d0 = (int)((r0[r] >> decal) & mask) - halfBg;
+                const int d1 = (int)((r1[r] >> decal) & mask) - halfBg;
+                v[r] = cmul(cpx<R>{(R)d0, (R)d1}, S.psi[t + 64 * r]);
+            }
+            fft512_forward(v, S.s, S.tw, t, S.bar_id);
+            const cpx<R>* g = gsw + (size_t)p * 2 * PARTS * kHalf;
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+#pragma unroll
+                for (int pt = 0; pt < PARTS; ++pt) {
+                    const cpx<R>* gk = g + (j * PARTS + pt) * kHalf;
+                    if constexpr (sizeof(R) == 4) {
+                        const float4* g4 = reinterpret_cast<const float4*>(gk);
+#pragma unroll
+                        for (int qq = 0; qq < 4; ++qq) {
+                            const float4 w = __ldg(g4 + qq * 64 + t);
+                            const cpx<R> k0 = {(R)w.x, (R)w.y}, k1 = {(R)w.z, (R)w.w};
+                            out[j][pt][2 * qq] = cadd(out[j][pt][2 * qq], cmul(v[2 * qq], k0));
+                            out[j][pt][2 * qq + 1] =
+                                cadd(out[j][pt][2 * qq + 1], cmul(v[2 * qq + 1], k1));
+                        }
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            const cpx<R> k0 = gk[key_index<R>(t, q)];
+                            out[j][pt][q] = cadd(out[j][pt][q], cmul(v[q], k0));
+                        }
+                    }
+                }
+        }
+    }
+
+    // back to the coefficient domain, one output polynomial at a time
+    const R inv = (R)(1.0 / 512.0);
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        uint32_t c0[8], c1[8];
+#pragma unroll
+        for (int pt = 0; pt < PARTS; ++pt) {
+            cpx<R> v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = out[j][pt][q];
+            fft512_inverse(v, S.s, S.tw, t, S.bar_id);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                cpx<R> z = cmulc(v[q], S.psi[t + 64 * q]);
+                const uint32_t a0 = (uint32_t)(uint64_t)to_int<R>(z.x * inv);
+                const uint32_t a1 = (uint32_t)(uint64_t)to_int<R>(z.y * inv);
+                if (PARTS == 1) {
+                    c0[q] = a0;
+                    c1[q] = a1;
+                } else if (pt == 0) {  // high part, scaled by 2^split
+                    c0[q] = a0 << S.split;
+                    c1[q] = a1 << S.split;
+                } else {
+                    c0[q] += a0;
+                    c1[q] += a1;
+                }
+            }
+        }
+        int32_t* dst = S.acc + j * kN;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int x0 = t + 64 * q;
+            if (ROT) {
+                dst[x0] = (int32_t)((uint32_t)dst[x0] + c0[q]);
+                dst[x0 + kHalf] = (int32_t)((uint32_t)dst[x0 + kHalf] + c1[q]);
+            } else {
+                dst[x0] = (int32_t)c0[q];
+                dst[x0 + kHalf] = (int32_t)c1[q];
+            }
+        }
+    }
+    group_sync(S.bar_id);
+}
+
+struct KParams {
+    int n, l, Bgbit, split;
+    uint32_t offset;
+};
+
+template <typename R, int PARTS, int MODE>
+__global__ void __launch_bounds__(256) k_external_product(KParams kp, Tables T, EpArgs a) {
+    extern __shared__ __align__(16) char smem[];
+    cpx<R>* tables = reinterpret_cast<cpx<R>*>(smem);
+    load_tables<R>(tables, T);
+    __syncthreads();
+
+    const int g = threadIdx.x >> 6;
+    const int t = threadIdx.x & 63;
+    const int groups = blockDim.x >> 6;
+    const int c = blockIdx.x * groups + g;
+    if (c >= a.count) return;
+
+    char* gbase = smem + SmemPlan<R>::tables + (size_t)g * SmemPlan<R>::group;
+    StepCtx<R, PARTS> S;
+    S.tw = tables;
+    S.psi = tables + 512;
+    S.acc = reinterpret_cast<int32_t*>(gbase);
+    S.s = scratch_at<R>(gbase + SmemPlan<R>::acc);
+    S.t = t;
+    S.bar_id = 1 + g;
+    S.l = kp.l;
+    S.Bgbit = kp.Bgbit;
+    S.split = kp.split;
+    S.offset = kp.offset;
+
+    const size_t gsw_elems = (size_t)2 * kp.l * 2 * PARTS * kHalf;
+    const cpx<R>* gsw_base = reinterpret_cast<const cpx<R>*>(a.gsw);
+
+    if (MODE == kEpBlindRotate) {
+        const int n = kp.n;
+        if (a.acc_in) {
+            const int32_t* src = a.acc_in + (size_t)c * 2 * kN;
+            for (int i = t; i < 2 * kN; i += 64) S.acc[i] = src[i];
+        } else {
+            // test vector mu * sum X^j rotated by X^{2N - barb}: the sign of
+            // coefficient x is + when (x + barb) mod 2N < N
+            const int32_t* xs = a.x + (size_t)c * (n + 1);
+            const int barb = mod_switch_2n(xs[n]);
+            for (int i = t; i < kN; i += 64) {
+                S.acc[i] = 0;
+                S.acc[kN + i] = (((i + barb) & (2 * kN - 1)) < kN) ? a.mu : -a.mu;
+            }
+        }
+        group_sync(S.bar_id);
+        const int32_t* bara = a.bara ? a.bara + (size_t)c * n : nullptr;
+        const int32_t* xs = a.x ? a.x + (size_t)c * (n + 1) : nullptr;
+        for (int i = 0; i < n; ++i) {
+            const int ai = bara ? bara[i] : mod_switch_2n(xs[i]);
+            if (ai == 0) continue;  // tfhe_blindRotate_FFT.cpp:114
+            ep_step<R, PARTS, true>(S, gsw_base + (size_t)i * gsw_elems, ai);
+        }
+        if (a.acc_out) {
+            int32_t* dst = a.acc_out + (size_t)c * 2 * kN;
+            for (int i = t; i < 2 * kN; i += 64) dst[i] = S.acc[i];
+        }
+        if (a.lwe_out) {
+            // tLweExtractLweSample: a'_0 = a_0, a'_j = -a_{N-j}, b' = b_0
+            int32_t* dst = a.lwe_out + (size_t)c * (kN + 1);
+            for (int i = t; i < kN; i += 64)
+                dst[i] = i == 0 ? S.acc[0] : (int32_t)(0u - (uint32_t)S.acc[kN - i]);
+            if (t == 0) dst[kN] = S.acc[kN];
+        }
+    } else {
+        const int32_t* src = a.acc_in + (size_t)c * 2 * kN;
+        for (int i = t; i < 2 * kN; i += 64) S.acc[i] = src[i];
+        group_sync(S.bar_id);
+        const cpx<R>* gsw = reinterpret_cast<const cpx<R>*>(
+            reinterpret_cast<const char*>(a.gsw) + a.gsw_stride * (size_t)c);
+        if (MODE == kEpPlain) {
+            ep_step<R, PARTS, false>(S, gsw, 0);
+        } else {
+            const int ai = a.bara[c];
+            if (ai != 0) ep_step<R, PARTS, true>(S, gsw, ai);
+        }
+        int32_t* dst = a.acc_out + (size_t)c * 2 * kN;
+        for (int i = t; i < 2 * kN; i += 64) dst[i] = S.acc[i];
+    }
+}
+
+// ----------------------------------------------------------------------
+// key conversion: one 64-thread group per polynomial
+// ----------------------------------------------------------------------
+__device__ __forceinline__ void twisted_forward64(const double* coef, cpx<double> (&v)[8],
+                                                  const FftScratch<double>& s,
+                                                  const cpx<double>* tw,
+                                                  const cpx<double>* psi, int t, int bar) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int x0 = t + 64 * r;
+        v[r] = cmul(cpx<double>{coef[x0], coef[x0 + kHalf]}, psi[x0]);
+    }
+    fft512_forward(v, s, tw, t, bar);
+}
+
+// Per polynomial smem: 1024 doubles of coefficients + scratch.
+constexpr size_t kConvGroupBytes = kN * sizeof(double) + 4 * kScratchStride * sizeof(double);
+
+template <int FORM>
+__global__ void __launch_bounds__(256) k_tgsw_to_fft(Tables T, const int32_t* __restrict__ in,
+                                                     void* out, int npoly, int split) {
+    extern __shared__ __align__(16) char smem[];
+    cpx<double>* tables = reinterpret_cast<cpx<double>*>(smem);
+    load_tables<double>(tables, T);
+    __syncthreads();
+    const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
+    const int poly = blockIdx.x * (blockDim.x >> 6) + g;
+    if (poly >= npoly) return;
+    char* gbase = smem + 1024 * sizeof(cpx<double>) + (size_t)g * kConvGroupBytes;
+    double* coef = reinterpret_cast<double*>(gbase);
+    FftScratch<double> s = scratch_at<double>(gbase + kN * sizeof(double));
+    const int32_t* src = in + (size_t)poly * kN;
+    const int bar = 1 + g;
+
+    if (FORM == kFormFp64) {
+        for (int i = t; i < kN; i += 64) coef[i] = (double)src[i];
+        group_sync(bar);
+        cpx<double> v[8];
+        twisted_forward64(coef, v, s, tables, tables + 512, t, bar);
+        cpx<double>* dst = reinterpret_cast<cpx<double>*>(out) + (size_t)poly * kHalf;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) dst[key_index<double>(t, q)] = v[q];
+    } else {
+        // split K = Khi * 2^s + Klo, Klo in [-2^(s-1), 2^(s-1))
+        cpx<float>* dst = reinterpret_cast<cpx<float>*>(out) + (size_t)poly * 2 * kHalf;
+        for (int part = 0; part < 2; ++part) {
+            for (int i = t; i < kN; i += 64) {
+                const int64_t K = src[i];
+                const int64_t half = (int64_t)1 << (split - 1);
+                const int64_t lo = ((K + half) & (((int64_t)1 << split) - 1)) - half;
+                const int64_t hi = (K - lo) >> split;
+                coef[i] = (double)(part == 0 ? hi : lo);
+            }
+            group_sync(bar);
+            cpx<double> v[8];
+            twisted_forward64(coef, v, s, tables, tables + 512, t, bar);
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                dst[part * kHalf + key_index<float>(t, q)] = {(float)v[q].x, (float)v[q].y};
+            group_sync(bar);
+        }
+    }
+}
+
+// engine FP64 layout -> integer coefficients (rounded to nearest)
+__global__ void __launch_bounds__(256) k_fft64_to_tgsw(Tables T, const void* in,
+                                                       int32_t* __restrict__ out, int npoly) {
+    extern __shared__ __align__(16) char smem[];
+    cpx<double>* tables = reinterpret_cast<cpx<double>*>(smem);
+    load_tables<double>(tables, T);
+    __syncthreads();
+    const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
+    const int poly = blockIdx.x * (blockDim.x >> 6) + g;
+    if (poly >= npoly) return;
+    char* gbase = smem + 1024 * sizeof(cpx<double>) + (size_t)g * kConvGroupBytes;
+    FftScratch<double> s = scratch_at<double>(gbase + kN * sizeof(double));
+    const cpx<double>* src = reinterpret_cast<const cpx<double>*>(in) + (size_t)poly * kHalf;
+    cpx<double> v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = src[key_index<double>(t, q)];
+    fft512_inverse(v, s, tables, t, 1 + g);
+    int32_t* dst = out + (size_t)poly * kN;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const cpx<double> z = cmulc(v[q], tables[512 + t + 64 * q]);
+        dst[t + 64 * q] = (int32_t)(uint32_t)(uint64_t)llrint(z.x / 512.0);
+        dst[t + 64 * q + kHalf] = (int32_t)(uint32_t)(uint64_t)llrint(z.y / 512.0);
+    }
+}
+
+// ----------------------------------------------------------------------
+// Lagrange half-complex form in the reference layout: value m' is
+// P(w^(2m'+1)), w = e^{i pi/N}.  Engine frequency m is P(psi^(4m+1)).
+// ----------------------------------------------------------------------
+__device__ __forceinline__ void engine_to_ref_index(int m, int* ref, bool* conj) {
+    const int e = (4 * m + 1) & 2047;
+    if (e < kN) {
+        *ref = (e - 1) >> 1;
+        *conj = false;
+    } else {
+        *ref = (2048 - e - 1) >> 1;
+        *conj = true;
+    }
+}
+
+// in: count polynomials (int32 coefficients), out: count x 512 complex
+// doubles in the reference layout, multiplied by `scale`.
+__global__ void __launch_bounds__(256) k_poly_to_lagrange(Tables T, const int32_t* __restrict__ in,
+                                                          double* __restrict__ out, int npoly,
+                                                          double scale) {
+    extern __shared__ __align__(16) char smem[];
+    cpx<double>* tables = reinterpret_cast<cpx<double>*>(smem);
+    load_tables<double>(tables, T);
+    __syncthreads();
+    const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
+    const int poly = blockIdx.x * (blockDim.x >> 6) + g;
+    if (poly >= npoly) return;
+    char* gbase = smem + 1024 * sizeof(cpx<double>) + (size_t)g * kConvGroupBytes;
+    double* coef = reinterpret_cast<double*>(gbase);
+    FftScratch<double> s = scratch_at<double>(gbase + kN * sizeof(double));
+    const int32_t* src = in + (size_t)poly * kN;
+    for (int i = t; i < kN; i += 64) coef[i] = (double)src[i];
+    group_sync(1 + g);
+    cpx<double> v[8];
+    twisted_forward64(coef, v, s, tables, tables + 512, t, 1 + g);
+    double* dst = out + (size_t)poly * kN;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        int ref;
+        bool cj;
+        engine_to_ref_index(freq_of(t, q), &ref, &cj);
+        dst[2 * ref] = v[q].x * scale;
+        dst[2 * ref + 1] = (cj ? -v[q].y : v[q].y) * scale;
+    }
+}
+
+// TorusPolynomial_fft: reference-layout values (torus / 2^32 scale) ->
+// Torus32 coefficients, truncating like TorusPolynomial_fft.cpp:39-41.
+__global__ void __launch_bounds__(256) k_lagrange_to_torus(Tables T, const double* __restrict__ in,
+                                                           int32_t* __restrict__ out, int npoly) {
+    extern __shared__ __align__(16) char smem[];
+    cpx<double>* tables = reinterpret_cast<cpx<double>*>(smem);
+    load_tables<double>(tables, T);
+    __syncthreads();
+    const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
+    const int poly = blockIdx.x * (blockDim.x >> 6) + g;
+    if (poly >= npoly) return;
+    char* gbase = smem + 1024 * sizeof(cpx<double>) + (size_t)g * kConvGroupBytes;
+    FftScratch<double> s = scratch_at<double>(gbase + kN * sizeof(double));
+    const double* src = in + (size_t)poly * kN;
+    cpx<double> v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        int ref;
+        bool cj;
+        engine_to_ref_index(freq_of(t, q), &ref, &cj);
+        const double re = src[2 * ref], im = src[2 * ref + 1];
+        v[q] = {re, cj ? -im : im};
+    }
+    fft512_inverse(v, s, tables, t, 1 + g);
+    const double sc = 4294967296.0 / 512.0;
+    int32_t* dst = out + (size_t)poly * kN;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const cpx<double> z = cmulc(v[q], tables[512 + t + 64 * q]);
+        dst[t + 64 * q] = (int32_t)(uint32_t)(uint64_t)__double2ll_rz(z.x * sc);
+        dst[t + 64 * q + kHalf] = (int32_t)(uint32_t)(uint64_t)__double2ll_rz(z.y * sc);
+    }
+}
+
+// reference layout <-> engine FP64 layout, values multiplied by `scale`
+__global__ void k_ref_to_engine64(const double* __restrict__ ref, cpx<double>* __restrict__ eng,
+                                  int npoly, double scale) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= npoly * kHalf) return;
+    const int poly = idx / kHalf, e = idx % kHalf;
+    const int t = e & 63, q = e >> 6;
+    int r;
+    bool cj;
+    engine_to_ref_index(freq_of(t, q), &r, &cj);
+    const double re = ref[(size_t)poly * kN + 2 * r], im = ref[(size_t)poly * kN + 2 * r + 1];
+    eng[(size_t)poly * kHalf + key_index<double>(t, q)] = {re * scale, (cj ? -im : im) * scale};
+}
+
+__global__ void k_engine64_to_ref(const cpx<double>* __restrict__ eng, double* __restrict__ ref,
+                                  int npoly, double scale) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= npoly * kHalf) return;
+    const int poly = idx / kHalf, e = idx % kHalf;
+    const int t = e & 63, q = e >> 6;
+    int r;
+    bool cj;
+    engine_to_ref_index(freq_of(t, q), &r, &cj);
+    const cpx<double> v = eng[(size_t)poly * kHalf + key_index<double>(t, q)];
+    ref[(size_t)poly * kN + 2 * r] = v.x * scale;
+    ref[(size_t)poly * kN + 2 * r + 1] = (cj ? -v.y : v.y) * scale;
+}
+
+// LagrangeHalfCPolynomialAddMul (tGswFFTExternMulToTLwe.cpp:172-180)
+__global__ void k_lagrange_addmul(const double* __restrict__ a, const double* __restrict__ b,
+                                  double* __restrict__ acc, size_t total) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const double ar = a[2 * i], ai = a[2 * i + 1], br = b[2 * i], bi = b[2 * i + 1];
+    acc[2 * i] += ar * br - ai * bi;
+    acc[2 * i + 1] += ar * bi + ai * br;
+}
+
+// ----------------------------------------------------------------------
+// small kernels
+// ----------------------------------------------------------------------
+__device__ __forceinline__ void gate_coeffs(int gate, int32_t e8, int32_t e4, int32_t* c,
+                                            int32_t* sa, int32_t* sb) {
+    switch (gate) {
+    case 0: *c = e8; *sa = -1; *sb = -1; break;   // NAND
+    case 1: *c = -e8; *sa = 1; *sb = 1; break;    // AND
+    case 2: *c = e8; *sa = 1; *sb = 1; break;     // OR
+    case 3: *c = e4; *sa = 2; *sb = 2; break;     // XOR
+    case 4: *c = -e4; *sa = -2; *sb = -2; break;  // XNOR
+    case 5: *c = -e8; *sa = -1; *sb = -1; break;  // NOR
+    case 6: *c = -e8; *sa = -1; *sb = 1; break;   // ANDNY
+    case 7: *c = -e8; *sa = 1; *sb = -1; break;   // ANDYN
+    case 8: *c = e8; *sa = -1; *sb = 1; break;    // ORNY
+    case 9: *c = e8; *sa = 1; *sb = -1; break;    // ORYN
+    default: *c = 0; *sa = 0; *sb = 0; break;
+    }
+}
+
+__global__ void k_gate_combine(int n, const int32_t* __restrict__ gates, int uniform_gate,
+                               const int32_t* __restrict__ ca, const int32_t* __restrict__ cb,
+                               int32_t* __restrict__ out, int count) {
+    const size_t width = (size_t)n + 1;
+    const size_t total = (size_t)count * width;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t c = idx / width;
+        const int i = (int)(idx - c * width);
+        const int gate = gates ? gates[c] : uniform_gate;
+        int32_t k0, sa, sb;
+        gate_coeffs(gate, 1 << 29, 1 << 30, &k0, &sa, &sb);
+        uint32_t v = (i == n) ? (uint32_t)k0 : 0u;
+        v += (uint32_t)sa * (uint32_t)ca[idx];
+        v += (uint32_t)sb * (uint32_t)cb[idx];
+        out[idx] = (int32_t)v;
+    }
+}
+
+__global__ void k_lwe_add2_const(const int32_t* __restrict__ u1, const int32_t* __restrict__ u2,
+                                 int32_t* __restrict__ out, int width, int32_t mu, int count) {
+    const size_t total = (size_t)count * width;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+        uint32_t v = (uint32_t)u1[i] + (uint32_t)u2[i];
+        if ((int)(i % width) == width - 1) v += (uint32_t)mu;
+        out[i] = (int32_t)v;
+    }
+}
+
+__global__ void k_mul_by_xai_minus_one(const int32_t* __restrict__ in,
+                                       const int32_t* __restrict__ ai, int32_t* __restrict__ out,
+                                       int polys_per_item, int count) {
+    const size_t total = (size_t)count * polys_per_item * kN;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t poly = idx / kN;
+        const int x = (int)(idx - poly * kN);
+        const int a = ai[poly / polys_per_item];
+        const int32_t* p = in + poly * kN;
+        out[idx] = (int32_t)((uint32_t)rot_coef(p, x, a) - (uint32_t)p[x]);
+    }
+}
+
+__global__ void k_extract(const int32_t* __restrict__ acc, int32_t* __restrict__ out, int count) {
+    const int c = blockIdx.x;
+    if (c >= count) return;
+    const int32_t* a = acc + (size_t)c * 2 * kN;
+    int32_t* o = out + (size_t)c * (kN + 1);
+    for (int i = threadIdx.x; i < kN; i += blockDim.x)
+        o[i] = i == 0 ? a[0] : (int32_t)(0u - (uint32_t)a[kN - i]);
+    if (threadIdx.x == 0) o[kN] = a[kN];
+}
+
+template <typename Kern>
+cudaError_t set_smem(Kern k, size_t bytes) {
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+uint32_t decomp_offset(int l, int Bgbit) {
+    // constants.h:24 (2164391936 for l = 3, Bgbit = 7)
+    uint32_t o = 0;
+    for (int i = 0; i < l; ++i) o += 1u << (32 - (i + 1) * Bgbit);
+    return o * (uint32_t)(1 << (Bgbit - 1));
+}
+
+template <typename R, int PARTS, int MODE>
+cudaError_t launch_ep_t(const DevParams& P, const Tables& T, const EpArgs& a, int groups,
+                        cudaStream_t st) {
+    if (a.count <= 0) return cudaSuccess;
+    KParams kp;
+    kp.n = P.n;
+    kp.l = P.l;
+    kp.Bgbit = P.Bgbit;
+    kp.split = P.split_bits;
+    kp.offset = decomp_offset(P.l, P.Bgbit);
+    const size_t smem = SmemPlan<R>::total(groups);
+    auto kern = k_external_product<R, PARTS, MODE>;
+    cudaError_t e = set_smem(kern, smem);
+    if (e != cudaSuccess) return e;
+    const int grid = (a.count + groups - 1) / groups;
+    kern<<<grid, 64 * groups, smem, st>>>(kp, T, a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------
+// host-side tables and launchers
+// ----------------------------------------------------------------------
+static void sincos_2pi_frac(long k, long M, double* c, double* s) {
+    k %= M;
+    const long q = (4 * k) / M;
+    const long r = k - q * (M / 4);
+    double cr, sr;
+    if (8 * r <= M) {
+        const double a = 2.0 * M_PI * (double)r / (double)M;
+        cr = cos(a);
+        sr = sin(a);
+    } else {
+        const double a = 2.0 * M_PI * (double)(M / 4 - r) / (double)M;
+        cr = sin(a);
+        sr = cos(a);
+    }
+    switch (q) {
+    case 0: *c = cr; *s = sr; break;
+    case 1: *c = -sr; *s = cr; break;
+    case 2: *c = -cr; *s = -sr; break;
+    default: *c = sr; *s = -cr; break;
+    }
+}
+
+void make_twiddles_host(double* h) {
+    for (int k = 0; k < 512; ++k) sincos_2pi_frac(k, 512, &h[2 * k], &h[2 * k + 1]);
+    for (int x = 0; x < 512; ++x) sincos_2pi_frac(x, 2048, &h[1024 + 2 * x], &h[1024 + 2 * x + 1]);
+}
+
+size_t tgsw_fft_bytes(const DevParams& P, Form f) {
+    const size_t rows = (size_t)(P.k + 1) * P.l;
+    if (f == kFormFp64) return rows * 2 * kHalf * sizeof(cpx<double>);
+    return rows * 2 * 2 * kHalf * sizeof(cpx<float>);
+}
+
+cudaError_t launch_tgsw_to_fft(const DevParams& P, Form f, const Tables& T, const int32_t* tgsw,
+                               void* out, int count, cudaStream_t st) {
+    const int npoly = count * (P.k + 1) * P.l * (P.k + 1);
+    if (npoly <= 0) return cudaSuccess;
+    const int groups = 4;
+    const size_t smem = 1024 * sizeof(cpx<double>) + groups * kConvGroupBytes;
+    const int grid = (npoly + groups - 1) / groups;
+    cudaError_t e;
+    if (f == kFormFp64) {
+        e = set_smem(k_tgsw_to_fft<kFormFp64>, smem);
+        if (e != cudaSuccess) return e;
+        k_tgsw_to_fft<kFormFp64><<<grid, 64 * groups, smem, st>>>(T, tgsw, out, npoly, 0);
+    } else {
+        e = set_smem(k_tgsw_to_fft<kFormSplitFp32>, smem);
+        if (e != cudaSuccess) return e;
+        k_tgsw_to_fft<kFormSplitFp32><<<grid, 64 * groups, smem, st>>>(T, tgsw, out, npoly,
+                                                                       P.split_bits);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tgsw_from_fft64(const DevParams& P, const Tables& T, const void* in,
+                                   int32_t* tgsw, int count, cudaStream_t st) {
+    const int npoly = count * (P.k + 1) * P.l * (P.k + 1);
+    if (npoly <= 0) return cudaSuccess;
+    const int groups = 4;
+    const size_t smem = 1024 * sizeof(cpx<double>) + groups * kConvGroupBytes;
+    cudaError_t e = set_smem(k_fft64_to_tgsw, smem);
+    if (e != cudaSuccess) return e;
+    k_fft64_to_tgsw<<<(npoly + groups - 1) / groups, 64 * groups, smem, st>>>(T, in, tgsw, npoly);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lagrange_ref_to_engine64(const double* ref, void* eng, int npoly, double scale,
+                                            cudaStream_t st) {
+    const int total = npoly * kHalf;
+    if (total <= 0) return cudaSuccess;
+    k_ref_to_engine64<<<(total + 255) / 256, 256, 0, st>>>(ref, reinterpret_cast<cpx<double>*>(eng),
+                                                          npoly, scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_engine64_to_lagrange_ref(const void* eng, double* ref, int npoly, double scale,
+                                            cudaStream_t st) {
+    const int total = npoly * kHalf;
+    if (total <= 0) return cudaSuccess;
+    k_engine64_to_ref<<<(total + 255) / 256, 256, 0, st>>>(
+        reinterpret_cast<const cpx<double>*>(eng), ref, npoly, scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_external_product(const DevParams& P, Form f, EpMode mode, const Tables& T,
+                                    const EpArgs& a, int groups, cudaStream_t st) {
+    if (groups < 1) groups = 1;
+    if (groups > 4) groups = 4;
+    if (f == kFormFp64) {
+        switch (mode) {
+        case kEpPlain: return launch_ep_t<double, 1, kEpPlain>(P, T, a, groups, st);
+        case kEpMuxRotate: return launch_ep_t<double, 1, kEpMuxRotate>(P, T, a, groups, st);
+        default: return launch_ep_t<double, 1, kEpBlindRotate>(P, T, a, groups, st);
+        }
+    }
+    switch (mode) {
+    case kEpPlain: return launch_ep_t<float, 2, kEpPlain>(P, T, a, groups, st);
+    case kEpMuxRotate: return launch_ep_t<float, 2, kEpMuxRotate>(P, T, a, groups, st);
+    default: return launch_ep_t<float, 2, kEpBlindRotate>(P, T, a, groups, st);
+    }
+}
+
+cudaError_t launch_gate_combine(const DevParams& P, const int32_t* gates, int32_t uniform_gate,
+                                const int32_t* ca, const int32_t* cb, int32_t* out, int count,
+                                cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    const size_t total = (size_t)count * (P.n + 1);
+    const int blocks = (int)((total + 255) / 256 < 8192 ? (total + 255) / 256 : 8192);
+    k_gate_combine<<<blocks, 256, 0, st>>>(P.n, gates, uniform_gate, ca, cb, out, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lwe_add2_const(const int32_t* u1, const int32_t* u2, int32_t* out,
+                                  int32_t width, int32_t mu, int count, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    const size_t total = (size_t)count * width;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    k_lwe_add2_const<<<blocks, 256, 0, st>>>(u1, u2, out, width, mu, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mul_by_xai_minus_one(const DevParams& P, const int32_t* in, const int32_t* ai,
+                                        int32_t* out, int count, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    const size_t total = (size_t)count * (P.k + 1) * kN;
+    const int blocks = (int)((total + 255) / 256 < 8192 ? (total + 255) / 256 : 8192);
+    k_mul_by_xai_minus_one<<<blocks, 256, 0, st>>>(in, ai, out, P.k + 1, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_extract(const DevParams& P, const int32_t* acc, int32_t* out, int count,
+                           cudaStream_t st) {
+    (void)P;
+    if (count <= 0) return cudaSuccess;
+    k_extract<<<count, 256, 0, st>>>(acc, out, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_poly_to_lagrange(const DevParams& P, const Tables& T, const int32_t* in,
+                                    double* out, int count, double scale, cudaStream_t st) {
+    (void)P;
+    if (count <= 0) return cudaSuccess;
+    const int groups = 4;
+    const size_t smem = 1024 * sizeof(cpx<double>) + groups * kConvGroupBytes;
+    cudaError_t e = set_smem(k_poly_to_lagrange, smem);
+    if (e != cudaSuccess) return e;
+    k_poly_to_lagrange<<<(count + groups - 1) / groups, 64 * groups, smem, st>>>(T, in, out, count,
+                                                                                 scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lagrange_to_torus(const DevParams& P, const Tables& T, const double* in,
+                                     int32_t* out, int count, cudaStream_t st) {
+    (void)P;
+    if (count <= 0) return cudaSuccess;
+    const int groups = 4;
+    const size_t smem = 1024 * sizeof(cpx<double>) + groups * kConvGroupBytes;
+    cudaError_t e = set_smem(k_lagrange_to_torus, smem);
+    if (e != cudaSuccess) return e;
+    k_lagrange_to_torus<<<(count + groups - 1) / groups, 64 * groups, smem, st>>>(T, in, out,
+                                                                                  count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lagrange_addmul(const double* a, const double* b, double* acc, int npoly,
+                                   int half, cudaStream_t st) {
+    const size_t total = (size_t)npoly * half;
+    if (total == 0) return cudaSuccess;
+    k_lagrange_addmul<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(a, b, acc, total);
+    return cudaGetLastError();
+}
+
+}  // namespace tfhe_gb300

@@ -1,0 +1,589 @@
+// capi.cpp -- implementation of the C ABI (include/tfhe_gpu.h).
+//
+// A context owns: the transform tables, the transform-domain bootstrapping
+// keys of the forms built, the padded key-switching table, reusable scratch
+// (gate combinations, extracted samples) and a stream.  Entry points check
+// their arguments, enqueue launches and return a status; the reference's
+// host instead exits the process on an OpenCL error (host.h:13-18).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/tfhe_gpu.h"
+#include "engine.h"
+
+using namespace tfhe_gb300;
+
+struct tfhe_gpu_ctx {
+    tfhe_params P;
+    DevParams dp;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void* d_tables = nullptr;  // 1024 double2 then 1024 float2
+    Tables tables{};
+    void* d_bk[kNumForms] = {nullptr, nullptr};
+    int32_t* d_ks = nullptr;
+    int32_t ks_row_stride = 0;
+    // scratch slots, grown on demand
+    void* d_scratch[4] = {nullptr, nullptr, nullptr, nullptr};
+    size_t scratch_bytes[4] = {0, 0, 0, 0};
+    int groups_per_cta[kNumForms] = {4, 4};
+    std::string last_error;
+    size_t key_bytes = 0;
+};
+
+namespace {
+
+tfhe_gpu_status fail(tfhe_gpu_ctx* ctx, tfhe_gpu_status s, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return s;
+}
+
+tfhe_gpu_status cuda_fail(tfhe_gpu_ctx* ctx, cudaError_t e, const char* where) {
+    std::string msg = std::string(where) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return fail(ctx, TFHE_GPU_OOM, msg);
+    if (e == cudaErrorInvalidValue) return fail(ctx, TFHE_GPU_BAD_PARAM, msg);
+    return fail(ctx, TFHE_GPU_DEVICE_ERROR, msg);
+}
+
+#define CK(ctx, expr)                                          \
+    do {                                                       \
+        cudaError_t e_ = (expr);                               \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #expr); \
+    } while (0)
+
+cudaStream_t pick(tfhe_gpu_ctx* ctx, void* stream) {
+    return stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->stream;
+}
+
+int32_t auto_split_bits(const tfhe_params& P) {
+    // The high part Khi of the key (32 - s bits) must make the FP32 product
+    // sum_p D_p * Khi_p exact after rounding: its size grows with the digit
+    // size (Bgbit) and the number of terms (N (k+1) l).  s = 24 keeps it
+    // below ~2^19 for the default set; every extra digit bit moves s up one.
+    int s = 24 + (P.Bgbit - 7);
+    if (P.l * (P.k + 1) > 6) s += 1;
+    if (s < 16) s = 16;
+    if (s > 30) s = 30;
+    return s;
+}
+
+bool params_supported(const tfhe_params* P, std::string* why) {
+    if (!P) { *why = "null params"; return false; }
+    if (P->N != 1024) { *why = "only N = 1024 is built"; return false; }
+    if (P->k != 1) { *why = "only k = 1 is built"; return false; }
+    if (P->n < 1 || P->n > 4096) { *why = "n out of range"; return false; }
+    if (P->l < 1 || P->l > 8 || P->Bgbit < 1 || P->l * P->Bgbit > 32) {
+        *why = "bad decomposition (l, Bgbit)";
+        return false;
+    }
+    if (P->ks_basebit < 1 || P->ks_basebit > 2 || P->ks_t < 1 || P->ks_t * P->ks_basebit > 31) {
+        *why = "bad key-switch decomposition (t, basebit <= 2)";
+        return false;
+    }
+    if (P->split_bits < 0 || P->split_bits > 31) { *why = "split_bits out of range"; return false; }
+    return true;
+}
+
+tfhe_gpu_status ensure_scratch(tfhe_gpu_ctx* ctx, int slot, size_t bytes, void** out) {
+    if (ctx->scratch_bytes[slot] < bytes) {
+        if (ctx->d_scratch[slot]) {
+            CK(ctx, cudaStreamSynchronize(ctx->stream));
+            cudaFree(ctx->d_scratch[slot]);
+            ctx->d_scratch[slot] = nullptr;
+            ctx->scratch_bytes[slot] = 0;
+        }
+        size_t want = bytes + bytes / 4;
+        CK(ctx, cudaMalloc(&ctx->d_scratch[slot], want));
+        ctx->scratch_bytes[slot] = want;
+    }
+    *out = ctx->d_scratch[slot];
+    return TFHE_GPU_OK;
+}
+
+bool form_ok(int32_t form) { return form == TFHE_GPU_FP64 || form == TFHE_GPU_SPLIT_FP32; }
+
+tfhe_gpu_status need_bk(tfhe_gpu_ctx* ctx, int32_t form) {
+    if (!form_ok(form)) return fail(ctx, TFHE_GPU_BAD_PARAM, "unknown form");
+    if (!ctx->d_bk[form]) return fail(ctx, TFHE_GPU_NO_KEY, "bootstrapping key of this form not uploaded");
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status set_device(tfhe_gpu_ctx* ctx) {
+    CK(ctx, cudaSetDevice(ctx->device));
+    return TFHE_GPU_OK;
+}
+
+#define CHECK_CTX(ctx)                                               \
+    do {                                                             \
+        if (!(ctx)) return TFHE_GPU_BAD_PARAM;                       \
+        tfhe_gpu_status s_ = set_device(ctx);                        \
+        if (s_ != TFHE_GPU_OK) return s_;                            \
+    } while (0)
+
+#define RET(s)                                   \
+    do {                                         \
+        tfhe_gpu_status r_ = (s);                \
+        if (r_ != TFHE_GPU_OK) return r_;        \
+    } while (0)
+
+// bootstrap without KS from LWE samples x into extracted samples u
+tfhe_gpu_status run_bootstrap_woks(tfhe_gpu_ctx* ctx, const int32_t* x, int32_t mu, int32_t* u,
+                                   int32_t count, int32_t form, cudaStream_t st) {
+    EpArgs a{};
+    a.x = x;
+    a.mu = mu;
+    a.lwe_out = u;
+    a.gsw = ctx->d_bk[form];
+    a.count = count;
+    CK(ctx, launch_external_product(ctx->dp, (Form)form, kEpBlindRotate, ctx->tables, a,
+                                    ctx->groups_per_cta[form], st));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status run_gates(tfhe_gpu_ctx* ctx, const int32_t* gates, int32_t uniform_gate,
+                          int32_t* out, const int32_t* ca, const int32_t* cb, int32_t count,
+                          int32_t form, cudaStream_t st) {
+    RET(need_bk(ctx, form));
+    if (!ctx->d_ks) return fail(ctx, TFHE_GPU_NO_KEY, "key-switching key not uploaded");
+    if (count == 0) return TFHE_GPU_OK;
+    const int n = ctx->P.n, nk = ctx->P.k * ctx->P.N;
+    void *x = nullptr, *u = nullptr;
+    RET(ensure_scratch(ctx, 0, (size_t)count * (n + 1) * sizeof(int32_t), &x));
+    RET(ensure_scratch(ctx, 1, (size_t)count * (nk + 1) * sizeof(int32_t), &u));
+    CK(ctx, launch_gate_combine(ctx->dp, gates, uniform_gate, ca, cb, (int32_t*)x, count, st));
+    const int32_t mu = tfhe_client_mod_switch_to_torus32(1, 8);
+    RET(run_bootstrap_woks(ctx, (const int32_t*)x, mu, (int32_t*)u, count, form, st));
+    CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, (const int32_t*)u, out, count,
+                             st));
+    return TFHE_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void tfhe_gpu_default_params(tfhe_params* out) {
+    if (!out) return;
+    std::memset(out, 0, sizeof(*out));
+    out->n = 630;
+    out->N = 1024;
+    out->k = 1;
+    out->l = 3;
+    out->Bgbit = 7;
+    out->ks_t = 8;
+    out->ks_basebit = 2;
+    out->split_bits = 0;
+    out->lwe_alpha = 1.0 / 32768.0;        // 2^-15
+    out->tlwe_alpha = 1.0 / 33554432.0;    // 2^-25
+}
+
+const char* tfhe_gpu_status_string(tfhe_gpu_status s) {
+    switch (s) {
+    case TFHE_GPU_OK: return "ok";
+    case TFHE_GPU_BAD_PARAM: return "bad parameter";
+    case TFHE_GPU_OOM: return "out of memory";
+    case TFHE_GPU_TIMEOUT: return "timeout";
+    case TFHE_GPU_DEVICE_ERROR: return "device error";
+    case TFHE_GPU_NO_KEY: return "key not uploaded";
+    }
+    return "unknown status";
+}
+
+tfhe_gpu_status tfhe_gpu_create(const tfhe_params* params, int32_t device, tfhe_gpu_ctx** out) {
+    if (!out) return TFHE_GPU_BAD_PARAM;
+    *out = nullptr;
+    std::string why;
+    if (!params_supported(params, &why)) return TFHE_GPU_BAD_PARAM;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+        return TFHE_GPU_DEVICE_ERROR;
+    tfhe_gpu_ctx* ctx = new tfhe_gpu_ctx();
+    ctx->P = *params;
+    if (ctx->P.split_bits == 0) ctx->P.split_bits = auto_split_bits(ctx->P);
+    ctx->dp = DevParams{ctx->P.n, ctx->P.N, ctx->P.k, ctx->P.l, ctx->P.Bgbit,
+                        ctx->P.ks_t, ctx->P.ks_basebit, ctx->P.split_bits};
+    ctx->device = device;
+    auto bail = [&](tfhe_gpu_status s) {
+        tfhe_gpu_destroy(ctx);
+        return s;
+    };
+    if (cudaSetDevice(device) != cudaSuccess) return bail(TFHE_GPU_DEVICE_ERROR);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(TFHE_GPU_DEVICE_ERROR);
+    std::vector<double> h64(2048);
+    make_twiddles_host(h64.data());
+    std::vector<float> h32(2048);
+    for (int i = 0; i < 2048; ++i) h32[i] = (float)h64[i];
+    const size_t b64 = 2048 * sizeof(double), b32 = 2048 * sizeof(float);
+    if (cudaMalloc(&ctx->d_tables, b64 + b32) != cudaSuccess) return bail(TFHE_GPU_OOM);
+    if (cudaMemcpy(ctx->d_tables, h64.data(), b64, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy((char*)ctx->d_tables + b64, h32.data(), b32, cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+        return bail(TFHE_GPU_DEVICE_ERROR);
+    ctx->tables.tw64 = ctx->d_tables;
+    ctx->tables.tw32 = (char*)ctx->d_tables + b64;
+    ctx->key_bytes = b64 + b32;
+    *out = ctx;
+    return TFHE_GPU_OK;
+}
+
+void tfhe_gpu_destroy(tfhe_gpu_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (int f = 0; f < kNumForms; ++f)
+        if (ctx->d_bk[f]) cudaFree(ctx->d_bk[f]);
+    if (ctx->d_ks) cudaFree(ctx->d_ks);
+    for (int s = 0; s < 4; ++s)
+        if (ctx->d_scratch[s]) cudaFree(ctx->d_scratch[s]);
+    if (ctx->d_tables) cudaFree(ctx->d_tables);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* tfhe_gpu_last_error(const tfhe_gpu_ctx* ctx) {
+    return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+tfhe_gpu_status tfhe_gpu_get_params(const tfhe_gpu_ctx* ctx, tfhe_params* out) {
+    if (!ctx || !out) return TFHE_GPU_BAD_PARAM;
+    *out = ctx->P;
+    return TFHE_GPU_OK;
+}
+
+void* tfhe_gpu_stream(const tfhe_gpu_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+tfhe_gpu_status tfhe_gpu_synchronize(tfhe_gpu_ctx* ctx) {
+    CHECK_CTX(ctx);
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return TFHE_GPU_OK;
+}
+
+size_t tfhe_gpu_tgsw_fft_bytes(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form) {
+    if (!ctx || !form_ok(form)) return 0;
+    return tgsw_fft_bytes(ctx->dp, (Form)form);
+}
+
+size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx) {
+    if (!ctx) return 0;
+    size_t b = ctx->key_bytes;
+    for (int s = 0; s < 4; ++s) b += ctx->scratch_bytes[s];
+    return b;
+}
+
+// ---- keys -------------------------------------------------------------
+
+static tfhe_gpu_status build_bk_forms(tfhe_gpu_ctx* ctx, const int32_t* d_bk_time,
+                                      uint32_t form_mask) {
+    for (int f = 0; f < kNumForms; ++f) {
+        if (!(form_mask & (1u << f))) continue;
+        const size_t bytes = (size_t)ctx->P.n * tgsw_fft_bytes(ctx->dp, (Form)f);
+        if (!ctx->d_bk[f]) {
+            CK(ctx, cudaMalloc(&ctx->d_bk[f], bytes));
+            ctx->key_bytes += bytes;
+        }
+        CK(ctx, launch_tgsw_to_fft(ctx->dp, (Form)f, ctx->tables, d_bk_time, ctx->d_bk[f],
+                                   ctx->P.n, ctx->stream));
+    }
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_upload_bootstrapping_key(tfhe_gpu_ctx* ctx, const int32_t* bk,
+                                                  uint32_t form_mask) {
+    CHECK_CTX(ctx);
+    if (!bk || (form_mask & ~3u) || !form_mask) return fail(ctx, TFHE_GPU_BAD_PARAM, "bk/form_mask");
+    const size_t words = (size_t)ctx->P.n * (ctx->P.k + 1) * ctx->P.l * (ctx->P.k + 1) * ctx->P.N;
+    int32_t* d = nullptr;
+    CK(ctx, cudaMalloc(&d, words * sizeof(int32_t)));
+    tfhe_gpu_status s = TFHE_GPU_OK;
+    cudaError_t e = cudaMemcpy(d, bk, words * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess)
+        s = cuda_fail(ctx, e, "copy bootstrapping key");
+    else
+        s = build_bk_forms(ctx, d, form_mask);
+    cudaFree(d);
+    return s;
+}
+
+tfhe_gpu_status tfhe_gpu_upload_bootstrapping_key_fft(tfhe_gpu_ctx* ctx, const double* bk_fft,
+                                                      uint32_t form_mask) {
+    CHECK_CTX(ctx);
+    if (!bk_fft || (form_mask & ~3u) || !form_mask)
+        return fail(ctx, TFHE_GPU_BAD_PARAM, "bk_fft/form_mask");
+    const int npoly = ctx->P.n * (ctx->P.k + 1) * ctx->P.l * (ctx->P.k + 1);
+    const size_t words = (size_t)npoly * ctx->P.N;
+    double* d_ref = nullptr;
+    void* d_eng = nullptr;
+    int32_t* d_time = nullptr;
+    tfhe_gpu_status s = TFHE_GPU_OK;
+    cudaError_t e = cudaMalloc(&d_ref, words * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_eng, words * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_time, words * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMemcpy(d_ref, bk_fft, words * sizeof(double), cudaMemcpyHostToDevice);
+    // reference values are torus/2^32: scale by 2^32 to integer units,
+    // transform back and round: the integer key is recovered exactly.
+    if (e == cudaSuccess)
+        e = launch_lagrange_ref_to_engine64(d_ref, d_eng, npoly, 4294967296.0, ctx->stream);
+    if (e == cudaSuccess)
+        e = launch_tgsw_from_fft64(ctx->dp, ctx->tables, d_eng, d_time,
+                                   npoly / ((ctx->P.k + 1) * ctx->P.l * (ctx->P.k + 1)), ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess)
+        s = cuda_fail(ctx, e, "import transform-domain bootstrapping key");
+    else
+        s = build_bk_forms(ctx, d_time, form_mask);
+    cudaFree(d_ref);
+    cudaFree(d_eng);
+    cudaFree(d_time);
+    return s;
+}
+
+tfhe_gpu_status tfhe_gpu_upload_keyswitch_key(tfhe_gpu_ctx* ctx, const int32_t* ks) {
+    CHECK_CTX(ctx);
+    if (!ks) return fail(ctx, TFHE_GPU_BAD_PARAM, "ks");
+    const int n = ctx->P.n;
+    const int stride = (n + 1 + 3) & ~3;
+    const size_t rows = (size_t)ctx->P.k * ctx->P.N * ctx->P.ks_t * (1 << ctx->P.ks_basebit);
+    if (!ctx->d_ks) {
+        CK(ctx, cudaMalloc(&ctx->d_ks, rows * stride * sizeof(int32_t)));
+        ctx->key_bytes += rows * stride * sizeof(int32_t);
+    }
+    ctx->ks_row_stride = stride;
+    CK(ctx, cudaMemset(ctx->d_ks, 0, rows * stride * sizeof(int32_t)));
+    CK(ctx, cudaMemcpy2D(ctx->d_ks, stride * sizeof(int32_t), ks, (n + 1) * sizeof(int32_t),
+                         (n + 1) * sizeof(int32_t), rows, cudaMemcpyHostToDevice));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_tgsw_to_fft(tfhe_gpu_ctx* ctx, const int32_t* tgsw, void* out,
+                                     int32_t count, tfhe_gpu_form form, void* stream) {
+    CHECK_CTX(ctx);
+    if (!form_ok(form) || count < 0 || (count && (!tgsw || !out)))
+        return fail(ctx, TFHE_GPU_BAD_PARAM, "tgsw_to_fft args");
+    CK(ctx, launch_tgsw_to_fft(ctx->dp, (Form)form, ctx->tables, tgsw, out, count, pick(ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+// ---- Lagrange processor ------------------------------------------------
+
+tfhe_gpu_status tfhe_gpu_IntPolynomial_ifft(tfhe_gpu_ctx* ctx, const int32_t* polys, double* out,
+                                            int32_t count, void* stream) {
+    CHECK_CTX(ctx);
+    if (count < 0 || (count && (!polys || !out))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    CK(ctx, launch_poly_to_lagrange(ctx->dp, ctx->tables, polys, out, count, 1.0, pick(ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_TorusPolynomial_ifft(tfhe_gpu_ctx* ctx, const int32_t* polys,
+                                              double* out, int32_t count, void* stream) {
+    CHECK_CTX(ctx);
+    if (count < 0 || (count && (!polys || !out))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    CK(ctx, launch_poly_to_lagrange(ctx->dp, ctx->tables, polys, out, count, 1.0 / 4294967296.0,
+                                    pick(ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_TorusPolynomial_fft(tfhe_gpu_ctx* ctx, const double* in, int32_t* polys,
+                                             int32_t count, void* stream) {
+    CHECK_CTX(ctx);
+    if (count < 0 || (count && (!polys || !in))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    CK(ctx, launch_lagrange_to_torus(ctx->dp, ctx->tables, in, polys, count, pick(ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_LagrangeHalfCPolynomialAddMul(tfhe_gpu_ctx* ctx, double* accum,
+                                                       const double* a, const double* b,
+                                                       int32_t count, void* stream) {
+    CHECK_CTX(ctx);
+    if (count < 0 || (count && (!accum || !a || !b))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    CK(ctx, launch_lagrange_addmul(a, b, accum, count, ctx->P.N / 2, pick(ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+// ---- hot path ------------------------------------------------------------
+
+tfhe_gpu_status tfhe_gpu_tLweMulByXaiMinusOne(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* ai,
+                                              const int32_t* in, int32_t count, void* stream) {
+    CHECK_CTX(ctx);
+    if (count < 0 || (count && (!out || !ai || !in))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    CK(ctx, launch_mul_by_xai_minus_one(ctx->dp, in, ai, out, count, pick(ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_tGswFFTExternMulToTLwe(tfhe_gpu_ctx* ctx, int32_t* accum, const void* gsw,
+                                                int32_t gsw_per_item, int32_t count,
+                                                tfhe_gpu_form form, void* stream) {
+    CHECK_CTX(ctx);
+    if (!form_ok(form) || count < 0 || (count && (!accum || !gsw)))
+        return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    EpArgs a{};
+    a.acc_in = accum;
+    a.acc_out = accum;
+    a.gsw = gsw;
+    a.gsw_stride = gsw_per_item ? tgsw_fft_bytes(ctx->dp, (Form)form) : 0;
+    a.count = count;
+    CK(ctx, launch_external_product(ctx->dp, (Form)form, kEpPlain, ctx->tables, a,
+                                    ctx->groups_per_cta[form], pick(ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_tfhe_MuxRotate_FFT(tfhe_gpu_ctx* ctx, int32_t* result,
+                                            const int32_t* accum, const void* gsw,
+                                            int32_t gsw_per_item, const int32_t* barai,
+                                            int32_t count, tfhe_gpu_form form, void* stream) {
+    CHECK_CTX(ctx);
+    if (!form_ok(form) || count < 0 || (count && (!result || !accum || !gsw || !barai)))
+        return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    EpArgs a{};
+    a.acc_in = accum;
+    a.acc_out = result;
+    a.bara = barai;
+    a.gsw = gsw;
+    a.gsw_stride = gsw_per_item ? tgsw_fft_bytes(ctx->dp, (Form)form) : 0;
+    a.count = count;
+    CK(ctx, launch_external_product(ctx->dp, (Form)form, kEpMuxRotate, ctx->tables, a,
+                                    ctx->groups_per_cta[form], pick(ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_tfhe_blindRotate_FFT(tfhe_gpu_ctx* ctx, int32_t* accum,
+                                              const int32_t* bara, int32_t count,
+                                              tfhe_gpu_form form, void* stream) {
+    CHECK_CTX(ctx);
+    RET(need_bk(ctx, form));
+    if (count < 0 || (count && (!accum || !bara))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    EpArgs a{};
+    a.acc_in = accum;
+    a.acc_out = accum;
+    a.bara = bara;
+    a.gsw = ctx->d_bk[form];
+    a.count = count;
+    CK(ctx, launch_external_product(ctx->dp, (Form)form, kEpBlindRotate, ctx->tables, a,
+                                    ctx->groups_per_cta[form], pick(ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_tLweExtractLweSample(tfhe_gpu_ctx* ctx, int32_t* out,
+                                              const int32_t* accum, int32_t count, void* stream) {
+    CHECK_CTX(ctx);
+    if (count < 0 || (count && (!out || !accum))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    CK(ctx, launch_extract(ctx->dp, accum, out, count, pick(ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_lweKeySwitch(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* in,
+                                      int32_t count, void* stream) {
+    CHECK_CTX(ctx);
+    if (!ctx->d_ks) return fail(ctx, TFHE_GPU_NO_KEY, "key-switching key not uploaded");
+    if (count < 0 || (count && (!out || !in))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, in, out, count,
+                             pick(ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_tfhe_bootstrap_woKS_FFT(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* x,
+                                                 int32_t mu, int32_t count, tfhe_gpu_form form,
+                                                 void* stream) {
+    CHECK_CTX(ctx);
+    RET(need_bk(ctx, form));
+    if (count < 0 || (count && (!out || !x))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    return run_bootstrap_woks(ctx, x, mu, out, count, form, pick(ctx, stream));
+}
+
+tfhe_gpu_status tfhe_gpu_tfhe_bootstrap_FFT(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* x,
+                                            int32_t mu, int32_t count, tfhe_gpu_form form,
+                                            void* stream) {
+    CHECK_CTX(ctx);
+    RET(need_bk(ctx, form));
+    if (!ctx->d_ks) return fail(ctx, TFHE_GPU_NO_KEY, "key-switching key not uploaded");
+    if (count < 0 || (count && (!out || !x))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    if (count == 0) return TFHE_GPU_OK;
+    void* u;
+    RET(ensure_scratch(ctx, 1, (size_t)count * (ctx->P.k * ctx->P.N + 1) * sizeof(int32_t), &u));
+    cudaStream_t st = pick(ctx, stream);
+    RET(run_bootstrap_woks(ctx, x, mu, (int32_t*)u, count, form, st));
+    CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, (const int32_t*)u, out, count,
+                             st));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_bootsGate(tfhe_gpu_ctx* ctx, int32_t gate, int32_t* out,
+                                   const int32_t* ca, const int32_t* cb, int32_t count,
+                                   tfhe_gpu_form form, void* stream) {
+    CHECK_CTX(ctx);
+    if (gate < 0 || gate > 9 || count < 0 || (count && (!out || !ca || !cb)))
+        return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    return run_gates(ctx, nullptr, gate, out, ca, cb, count, form, pick(ctx, stream));
+}
+
+tfhe_gpu_status tfhe_gpu_bootsGates(tfhe_gpu_ctx* ctx, const int32_t* gates, int32_t* out,
+                                    const int32_t* ca, const int32_t* cb, int32_t count,
+                                    tfhe_gpu_form form, void* stream) {
+    CHECK_CTX(ctx);
+    if (count < 0 || (count && (!gates || !out || !ca || !cb)))
+        return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    return run_gates(ctx, gates, 0, out, ca, cb, count, form, pick(ctx, stream));
+}
+
+tfhe_gpu_status tfhe_gpu_bootsMUX(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* a,
+                                  const int32_t* b, const int32_t* c, int32_t count,
+                                  tfhe_gpu_form form, void* stream) {
+    CHECK_CTX(ctx);
+    RET(need_bk(ctx, form));
+    if (!ctx->d_ks) return fail(ctx, TFHE_GPU_NO_KEY, "key-switching key not uploaded");
+    if (count < 0 || (count && (!out || !a || !b || !c))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    if (count == 0) return TFHE_GPU_OK;
+    const int n = ctx->P.n, nk = ctx->P.k * ctx->P.N;
+    cudaStream_t st = pick(ctx, stream);
+    void *x = nullptr, *u = nullptr, *s = nullptr;
+    RET(ensure_scratch(ctx, 0, (size_t)2 * count * (n + 1) * sizeof(int32_t), &x));
+    RET(ensure_scratch(ctx, 1, (size_t)2 * count * (nk + 1) * sizeof(int32_t), &u));
+    RET(ensure_scratch(ctx, 2, (size_t)count * (nk + 1) * sizeof(int32_t), &s));
+    int32_t* x1 = (int32_t*)x;
+    int32_t* x2 = x1 + (size_t)count * (n + 1);
+    // upstream bootsMUX: AND(a, b) and AND(not a, c) bootstrapped without
+    // key switch, added with (0, 1/8), then one key switch.
+    CK(ctx, launch_gate_combine(ctx->dp, nullptr, TFHE_GATE_AND, a, b, x1, count, st));
+    CK(ctx, launch_gate_combine(ctx->dp, nullptr, TFHE_GATE_ANDNY, a, c, x2, count, st));
+    const int32_t mu = tfhe_client_mod_switch_to_torus32(1, 8);
+    RET(run_bootstrap_woks(ctx, x1, mu, (int32_t*)u, 2 * count, form, st));
+    const int32_t* u1 = (const int32_t*)u;
+    const int32_t* u2 = u1 + (size_t)count * (nk + 1);
+    CK(ctx, launch_lwe_add2_const(u1, u2, (int32_t*)s, nk + 1, mu, count, st));
+    CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, (const int32_t*)s, out, count,
+                             st));
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_bootsGates_host(tfhe_gpu_ctx* ctx, const int32_t* gates,
+                                         int32_t uniform_gate, int32_t* out, const int32_t* ca,
+                                         const int32_t* cb, int32_t count, tfhe_gpu_form form) {
+    CHECK_CTX(ctx);
+    if (count < 0 || (count && (!out || !ca || !cb))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    if (!gates && (uniform_gate < 0 || uniform_gate > 9)) return fail(ctx, TFHE_GPU_BAD_PARAM, "gate");
+    if (count == 0) return TFHE_GPU_OK;
+    const size_t w = (size_t)ctx->P.n + 1;
+    const size_t lwe_bytes = (size_t)count * w * sizeof(int32_t);
+    void *d_io = nullptr, *d_g = nullptr;
+    RET(ensure_scratch(ctx, 3, 3 * lwe_bytes + (gates ? count * sizeof(int32_t) : 0), &d_io));
+    int32_t* d_ca = (int32_t*)d_io;
+    int32_t* d_cb = d_ca + (size_t)count * w;
+    int32_t* d_out = d_cb + (size_t)count * w;
+    if (gates) d_g = d_out + (size_t)count * w;
+    cudaStream_t st = ctx->stream;
+    CK(ctx, cudaMemcpyAsync(d_ca, ca, lwe_bytes, cudaMemcpyHostToDevice, st));
+    CK(ctx, cudaMemcpyAsync(d_cb, cb, lwe_bytes, cudaMemcpyHostToDevice, st));
+    if (gates) CK(ctx, cudaMemcpyAsync(d_g, gates, count * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    RET(run_gates(ctx, (const int32_t*)d_g, uniform_gate, d_out, d_ca, d_cb, count, form, st));
+    CK(ctx, cudaMemcpyAsync(out, d_out, lwe_bytes, cudaMemcpyDeviceToHost, st));
+    CK(ctx, cudaStreamSynchronize(st));
+    return TFHE_GPU_OK;
+}
+
+}  // extern "C"

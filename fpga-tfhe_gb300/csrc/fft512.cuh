@@ -1,0 +1,198 @@
+// fft512.cuh -- negacyclic transform for N = 1024 as a 512-point complex FFT.
+//
+// A real polynomial a(X) mod X^1024 + 1 is folded into z_j = a_j + i a_{j+512}
+// (j < 512) and twisted by psi^j, psi = e^{i pi / 1024}.  The 512-point DFT
+// with kernel W = e^{+2 pi i / 512} then gives Z_m = a(psi^(4m+1)): the
+// evaluations of a at half of the odd 2048-th roots of unity; the other half
+// are their conjugates.  The reference computes the same evaluations with a
+// 2048-point transform of the antiperiodic extension
+// (tfhe_blindRotate_FFT/tGswFFTExternMulToTLwe.cpp:97-130, "ifft") and with a
+// Hermitian placement on the way back (TorusPolynomial_fft.cpp:4-43); this
+// form does a quarter of that work.
+//
+// Work split: 64 threads (two warps) per transform, 8 points per thread,
+// three radix-8 passes in registers with two exchanges through shared memory.
+//   forward (decimation in frequency):
+//     pass A  thread t: points t + 64r            -> out positions t + 64q
+//     pass B  thread t=(b,j): 64b + j + 8r          -> 64b + j + 8q
+//     pass C  thread t: 8t + r                      -> 8t + q (registers)
+//   position 64qA + 8qB + qC holds frequency qA + 8qB + 64qC.  The pointwise
+//   product works in that order; the key is stored in it, so no reordering.
+//   inverse (decimation in time) runs the passes backwards, input from
+//   registers (positions 8t + q) to natural order (positions t + 64q).
+// Shared scratch: two ping-pong buffers, split re/im, padded p + p/8 so the
+// strided exchanges are (almost) free of bank conflicts.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tfhe_gb300 {
+
+template <typename R>
+struct cpx {
+    R x, y;
+};
+
+template <typename R>
+__device__ __forceinline__ cpx<R> cadd(cpx<R> a, cpx<R> b) {
+    return {a.x + b.x, a.y + b.y};
+}
+template <typename R>
+__device__ __forceinline__ cpx<R> csub(cpx<R> a, cpx<R> b) {
+    return {a.x - b.x, a.y - b.y};
+}
+template <typename R>
+__device__ __forceinline__ cpx<R> cmul(cpx<R> a, cpx<R> b) {
+    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+// a * conj(b)
+template <typename R>
+__device__ __forceinline__ cpx<R> cmulc(cpx<R> a, cpx<R> b) {
+    return {a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
+}
+
+constexpr int kFftPoints = 512;
+constexpr int kFftThreads = 64;
+constexpr int kScratchStride = 576;  // 512 + 512/8 padding
+
+__device__ __forceinline__ int spad(int p) { return p + (p >> 3); }
+
+// 8-point DFT, y_q = sum_r v_r w^{rq}, w = e^{S 2 pi i / 8}.
+template <int S, typename R>
+__device__ __forceinline__ void dft8(cpx<R> (&v)[8]) {
+    const R h = (R)0.70710678118654752440084436210485;
+    cpx<R> b[8];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        b[r] = cadd(v[r], v[r + 4]);
+        b[r + 4] = csub(v[r], v[r + 4]);
+    }
+    {  // b5 *= w = (1 + S i) h
+        const R x = b[5].x, y = b[5].y;
+        b[5] = {(x - S * y) * h, (y + S * x) * h};
+    }
+    {  // b6 *= w^2 = S i
+        const R x = b[6].x, y = b[6].y;
+        b[6] = {-S * y, S * x};
+    }
+    {  // b7 *= w^3 = (-1 + S i) h
+        const R x = b[7].x, y = b[7].y;
+        b[7] = {(-x - S * y) * h, (S * x - y) * h};
+    }
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const cpx<R> c0 = b[4 * half + 0], c1 = b[4 * half + 1];
+        const cpx<R> c2 = b[4 * half + 2], c3 = b[4 * half + 3];
+        const cpx<R> e0 = cadd(c0, c2), e1 = csub(c0, c2), e2 = cadd(c1, c3);
+        const cpx<R> d = csub(c1, c3);
+        const cpx<R> e3 = {-S * d.y, S * d.x};
+        v[half + 0] = cadd(e0, e2);
+        v[half + 2] = cadd(e1, e3);
+        v[half + 4] = csub(e0, e2);
+        v[half + 6] = csub(e1, e3);
+    }
+}
+
+__device__ __forceinline__ void group_sync(int bar_id) {
+    asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(kFftThreads) : "memory");
+}
+
+template <typename R>
+struct FftScratch {
+    R* re0;
+    R* im0;
+    R* re1;
+    R* im1;
+};
+
+template <typename R>
+__device__ __forceinline__ void sst(R* re, R* im, int p, cpx<R> v) {
+    const int q = spad(p);
+    re[q] = v.x;
+    im[q] = v.y;
+}
+template <typename R>
+__device__ __forceinline__ cpx<R> sld(const R* re, const R* im, int p) {
+    const int q = spad(p);
+    return {re[q], im[q]};
+}
+
+// Forward transform.  In: v[r] = z[t + 64r].  Out: v[q] = position 8t + q.
+// tw[k] = e^{+2 pi i k / 512}.
+template <typename R>
+__device__ __forceinline__ void fft512_forward(cpx<R> (&v)[8], const FftScratch<R>& s,
+                                               const cpx<R>* __restrict__ tw, int t,
+                                               int bar_id) {
+    // pass A
+    dft8<1>(v);
+#pragma unroll
+    for (int q = 1; q < 8; ++q) v[q] = cmul(v[q], tw[(t * q) & 511]);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sst(s.re0, s.im0, t + 64 * q, v[q]);
+    group_sync(bar_id);
+    // pass B
+    const int b = t >> 3, j = t & 7;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = sld(s.re0, s.im0, 64 * b + j + 8 * r);
+    dft8<1>(v);
+#pragma unroll
+    for (int q = 1; q < 8; ++q) v[q] = cmul(v[q], tw[(8 * j * q) & 511]);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sst(s.re1, s.im1, 64 * b + j + 8 * q, v[q]);
+    group_sync(bar_id);
+    // pass C
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = sld(s.re1, s.im1, 8 * t + r);
+    dft8<1>(v);
+}
+
+// Inverse transform (unnormalised: returns 512 z).  In: v[q] = position
+// 8t + q.  Out: v[q] = z[t + 64q].
+template <typename R>
+__device__ __forceinline__ void fft512_inverse(cpx<R> (&v)[8], const FftScratch<R>& s,
+                                               const cpx<R>* __restrict__ tw, int t,
+                                               int bar_id) {
+    // pass C'
+    dft8<-1>(v);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sst(s.re0, s.im0, 8 * t + q, v[q]);
+    group_sync(bar_id);
+    // pass B'
+    const int b = t >> 3, j = t & 7;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        v[r] = sld(s.re0, s.im0, 64 * b + j + 8 * r);
+        if (r) v[r] = cmulc(v[r], tw[(8 * j * r) & 511]);
+    }
+    dft8<-1>(v);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sst(s.re1, s.im1, 64 * b + j + 8 * q, v[q]);
+    group_sync(bar_id);
+    // pass A'
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        v[r] = sld(s.re1, s.im1, t + 64 * r);
+        if (r) v[r] = cmulc(v[r], tw[(t * r) & 511]);
+    }
+    dft8<-1>(v);
+}
+
+// Frequency held at (thread t, register q) after the forward transform.
+__host__ __device__ __forceinline__ int freq_of(int t, int q) {
+    return (t >> 3) + 8 * (t & 7) + 64 * q;
+}
+
+// Storage index of (thread t, register q) in one 512-point key polynomial.
+// FP32: pairs of complex per 16-byte load, [q/2][t][q%2]; FP64: [q][t].
+template <typename R>
+__host__ __device__ __forceinline__ int key_index(int t, int q);
+template <>
+__host__ __device__ __forceinline__ int key_index<float>(int t, int q) {
+    return ((q >> 1) * 64 + t) * 2 + (q & 1);
+}
+template <>
+__host__ __device__ __forceinline__ int key_index<double>(int t, int q) {
+    return q * 64 + t;
+}
+
+}  // namespace tfhe_gb300

@@ -1,0 +1,242 @@
+/*
+ * tfhe_gpu.h -- C ABI of the GB300 TFHE gate-bootstrapping engine.
+ *
+ * The engine is the GPU replacement of the TFHE bootstrapping path of
+ * shreks99/fpga-tfhe.  Every entry point below names the reference function
+ * it replaces (paths inside that project).  Conventions:
+ *   - plain pointers and sizes, no C++ types;
+ *   - "device batch" entry points take DEVICE pointers (cudaMalloc'd or from
+ *     any allocator) to `count` items laid out back to back and a CUDA stream
+ *     (cudaStream_t passed as void*, NULL = the context's stream); they
+ *     enqueue work and return without synchronising;
+ *   - "_host" entry points take HOST buffers, copy in, compute, copy out and
+ *     synchronise (the end-to-end form a drop-in caller uses);
+ *   - every call returns a status; nothing exits the process (the reference
+ *     host exits on OpenCL errors, kernel/src/include/host.h:13-18);
+ *   - a context owns its device memory (keys, tables, scratch); one context
+ *     per host thread, or serialise calls externally.
+ *
+ * Data layouts (int32 = Torus32, arithmetic mod 2^32):
+ *   LWE sample        int32[n + 1]             a[0..n-1], b
+ *   extracted sample  int32[k N + 1]
+ *   TLWE sample       int32[(k + 1) N]          a[0..k-1], then b
+ *   TGSW sample       int32[(k+1) l][(k+1)][N]  row p = i l + j
+ *   bootstrapping key n TGSW samples of the bits of the LWE key
+ *   key-switching key int32[k N][t][2^basebit][n + 1]
+ *   Lagrange polynomial double[N/2][2]: values at w^(2m+1), w = e^{i pi/N}
+ *                      (the reference's LagrangeHalfCPolynomial_FPGA,
+ *                      kernel/src/include/polynomials.h:15-17)
+ */
+#ifndef TFHE_GPU_H
+#define TFHE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tfhe_gpu_status {
+    TFHE_GPU_OK = 0,
+    TFHE_GPU_BAD_PARAM = 1,    /* invalid argument or unsupported parameter set */
+    TFHE_GPU_OOM = 2,          /* device or pinned host allocation failed       */
+    TFHE_GPU_TIMEOUT = 3,      /* a bounded device wait gave up                 */
+    TFHE_GPU_DEVICE_ERROR = 4, /* CUDA reported an error (see last_error)       */
+    TFHE_GPU_NO_KEY = 5        /* the key needed by the call was not uploaded   */
+} tfhe_gpu_status;
+
+/* Precision form of the negacyclic transform. */
+typedef enum tfhe_gpu_form {
+    TFHE_GPU_FP64 = 0,       /* FP64 transform, reference truncating rounding  */
+    TFHE_GPU_SPLIT_FP32 = 1  /* FP32 transform; key split K = Khi 2^s + Klo    */
+} tfhe_gpu_form;
+
+#define TFHE_GPU_FORM_MASK(f) (1u << (f))
+
+/* Gate identifiers of the batched gate entry points. */
+typedef enum tfhe_gpu_gate {
+    TFHE_GATE_NAND = 0, TFHE_GATE_AND = 1, TFHE_GATE_OR = 2, TFHE_GATE_XOR = 3,
+    TFHE_GATE_XNOR = 4, TFHE_GATE_NOR = 5, TFHE_GATE_ANDNY = 6,
+    TFHE_GATE_ANDYN = 7, TFHE_GATE_ORNY = 8, TFHE_GATE_ORYN = 9
+} tfhe_gpu_gate;
+
+/* Parameter set (kernel/src/include/constants.h:26-53). */
+typedef struct tfhe_params {
+    int32_t n;          /* LWE dimension (630)                     */
+    int32_t N;          /* ring degree (1024; the only one built)  */
+    int32_t k;          /* TLWE mask polynomials (1)               */
+    int32_t l;          /* decomposition length (3)                */
+    int32_t Bgbit;      /* log2 decomposition base (7)             */
+    int32_t ks_t;       /* key-switch length (8)                   */
+    int32_t ks_basebit; /* log2 key-switch base (2)                */
+    int32_t split_bits; /* s of the split-FP32 key split; 0 = auto */
+    double lwe_alpha;   /* LWE / key-switch noise stdev            */
+    double tlwe_alpha;  /* TLWE / bootstrapping key noise stdev    */
+} tfhe_params;
+
+typedef struct tfhe_gpu_ctx tfhe_gpu_ctx;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* The 110-bit default gate set of the reference (constants.h:26-40). */
+void tfhe_gpu_default_params(tfhe_params* out);
+/* Create a context on `device`; uploads the transform tables. */
+tfhe_gpu_status tfhe_gpu_create(const tfhe_params* params, int32_t device,
+                                tfhe_gpu_ctx** out);
+void tfhe_gpu_destroy(tfhe_gpu_ctx* ctx);
+const char* tfhe_gpu_status_string(tfhe_gpu_status s);
+/* Human-readable detail of the last failure on this context. */
+const char* tfhe_gpu_last_error(const tfhe_gpu_ctx* ctx);
+/* The parameters in use (split_bits resolved). */
+tfhe_gpu_status tfhe_gpu_get_params(const tfhe_gpu_ctx* ctx, tfhe_params* out);
+/* The context's own stream (as void*). */
+void* tfhe_gpu_stream(const tfhe_gpu_ctx* ctx);
+/* Wait for all work of the context's stream. */
+tfhe_gpu_status tfhe_gpu_synchronize(tfhe_gpu_ctx* ctx);
+/* Bytes of one TGSW sample in the engine's transform layout. */
+size_t tfhe_gpu_tgsw_fft_bytes(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form);
+/* Device bytes the context holds (keys, tables, scratch). */
+size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
+
+/* ---- keys --------------------------------------------------------------- */
+
+/* Upload the bootstrapping key in the time domain (host int32,
+ * n x TGSW) and build the transform-domain copies of the forms in
+ * `form_mask`.  Replaces the key the reference hands to the FPGA as
+ * TGswSampleFFT_FPGA[n] (tfhe_blindRotate_FFT_tb.cpp:295-297, 342). */
+tfhe_gpu_status tfhe_gpu_upload_bootstrapping_key(tfhe_gpu_ctx* ctx,
+                                                  const int32_t* bk,
+                                                  uint32_t form_mask);
+/* Upload the bootstrapping key in the reference's transform format:
+ * n x (k+1)l x (k+1) Lagrange polynomials, values of torus/2^32 at
+ * w^(2m+1) (the a[] arrays of TGswSampleFFT_FPGA, tgswsample.h:8-16). */
+tfhe_gpu_status tfhe_gpu_upload_bootstrapping_key_fft(tfhe_gpu_ctx* ctx,
+                                                      const double* bk_fft,
+                                                      uint32_t form_mask);
+/* Upload the key-switching key (host int32 [kN][t][base][n+1]),
+ * lwe-keyswitch-functions.cpp:85-99, 163-215. */
+tfhe_gpu_status tfhe_gpu_upload_keyswitch_key(tfhe_gpu_ctx* ctx, const int32_t* ks);
+
+/* TGSW samples (device, count x TGSW int32) -> engine transform layout
+ * (device, count x tfhe_gpu_tgsw_fft_bytes). Upstream tGswToFftConvert. */
+tfhe_gpu_status tfhe_gpu_tgsw_to_fft(tfhe_gpu_ctx* ctx, const int32_t* tgsw,
+                                     void* out, int32_t count,
+                                     tfhe_gpu_form form, void* stream);
+
+/* ---- Lagrange processor (FFT processor of LagrangeHalfCPolynomial) ----- */
+
+/* IntPolynomial -> Lagrange (tGswFFTExternMulToTLwe.cpp:97-130, the correct
+ * form of IntPolynomial_ifft, IntPolynomial_ifft.cpp:5-29). Device batch. */
+tfhe_gpu_status tfhe_gpu_IntPolynomial_ifft(tfhe_gpu_ctx* ctx, const int32_t* polys,
+                                            double* out, int32_t count, void* stream);
+/* TorusPolynomial -> Lagrange, torus/2^32 scale (upstream
+ * TorusPolynomial_ifft, the key conversion). Device batch. */
+tfhe_gpu_status tfhe_gpu_TorusPolynomial_ifft(tfhe_gpu_ctx* ctx, const int32_t* polys,
+                                              double* out, int32_t count, void* stream);
+/* Lagrange -> TorusPolynomial, truncating (TorusPolynomial_fft.cpp:4-43,
+ * tLweFromFFTConvert.cpp:4-24). Device batch. */
+tfhe_gpu_status tfhe_gpu_TorusPolynomial_fft(tfhe_gpu_ctx* ctx, const double* in,
+                                             int32_t* polys, int32_t count, void* stream);
+/* accum += a * b pointwise (tGswFFTExternMulToTLwe.cpp:172-180). */
+tfhe_gpu_status tfhe_gpu_LagrangeHalfCPolynomialAddMul(tfhe_gpu_ctx* ctx, double* accum,
+                                                       const double* a, const double* b,
+                                                       int32_t count, void* stream);
+
+/* ---- hot path ------------------------------------------------------------ */
+
+/* out = (X^{a_i} - 1) in, per TLWE sample i (tfhe_MuxRotate_FFT.cpp:5-33). */
+tfhe_gpu_status tfhe_gpu_tLweMulByXaiMinusOne(tfhe_gpu_ctx* ctx, int32_t* out,
+                                              const int32_t* ai, const int32_t* in,
+                                              int32_t count, void* stream);
+/* accum_i <- TGSW_i [x] accum_i (tGswFFTExternMulToTLwe.cpp:203-247).
+ * gsw: engine layout (tfhe_gpu_tgsw_to_fft), `gsw_per_item` 1 = one TGSW
+ * per sample, 0 = one TGSW shared by all. In place on device TLWEs. */
+tfhe_gpu_status tfhe_gpu_tGswFFTExternMulToTLwe(tfhe_gpu_ctx* ctx, int32_t* accum,
+                                                const void* gsw, int32_t gsw_per_item,
+                                                int32_t count, tfhe_gpu_form form,
+                                                void* stream);
+/* result_i = TGSW_i [x] ((X^{a_i} - 1) accum_i) + accum_i
+ * (tfhe_MuxRotate_FFT.cpp:56-85). */
+tfhe_gpu_status tfhe_gpu_tfhe_MuxRotate_FFT(tfhe_gpu_ctx* ctx, int32_t* result,
+                                            const int32_t* accum, const void* gsw,
+                                            int32_t gsw_per_item, const int32_t* barai,
+                                            int32_t count, tfhe_gpu_form form,
+                                            void* stream);
+/* Blind rotation of each accumulator by its bara[n] with the context's
+ * bootstrapping key, all n steps, skipping bara_i = 0
+ * (tfhe_blindRotate_FFT.cpp:61-147). In place. */
+tfhe_gpu_status tfhe_gpu_tfhe_blindRotate_FFT(tfhe_gpu_ctx* ctx, int32_t* accum,
+                                              const int32_t* bara, int32_t count,
+                                              tfhe_gpu_form form, void* stream);
+/* Sample extraction TLWE -> LWE(kN) (upstream tLweExtractLweSample). */
+tfhe_gpu_status tfhe_gpu_tLweExtractLweSample(tfhe_gpu_ctx* ctx, int32_t* out,
+                                              const int32_t* accum, int32_t count,
+                                              void* stream);
+/* Key switch LWE(kN) -> LWE(n) with the context's key
+ * (lwe-keyswitch-functions.cpp:228-241). */
+tfhe_gpu_status tfhe_gpu_lweKeySwitch(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* in,
+                                      int32_t count, void* stream);
+/* Bootstrap without key switch: LWE(n) -> LWE(kN) with test vector mu
+ * (upstream tfhe_bootstrap_woKS_FFT; front end
+ * tfhe_bootstrap_woKS_FFT.cpp:27-73, mulByXaiOrCopy.cpp:3-44). */
+tfhe_gpu_status tfhe_gpu_tfhe_bootstrap_woKS_FFT(tfhe_gpu_ctx* ctx, int32_t* out,
+                                                 const int32_t* x, int32_t mu,
+                                                 int32_t count, tfhe_gpu_form form,
+                                                 void* stream);
+/* Full bootstrap LWE(n) -> LWE(n) (upstream tfhe_bootstrap_FFT). */
+tfhe_gpu_status tfhe_gpu_tfhe_bootstrap_FFT(tfhe_gpu_ctx* ctx, int32_t* out,
+                                            const int32_t* x, int32_t mu, int32_t count,
+                                            tfhe_gpu_form form, void* stream);
+
+/* ---- gates (the calls of test_bench/server/cloud.c:10-35) ------------- */
+
+/* Batched gates, one gate type for all: out_i = GATE(ca_i, cb_i).
+ * Upstream bootsNAND/AND/OR/XOR/... ; the OR linear combination is
+ * tfhe_blindRotate_FFT_tb.cpp:267-276. Device batch. */
+tfhe_gpu_status tfhe_gpu_bootsGate(tfhe_gpu_ctx* ctx, int32_t gate, int32_t* out,
+                                   const int32_t* ca, const int32_t* cb, int32_t count,
+                                   tfhe_gpu_form form, void* stream);
+/* Batched gates with a gate id per item (device int32[count]). */
+tfhe_gpu_status tfhe_gpu_bootsGates(tfhe_gpu_ctx* ctx, const int32_t* gates, int32_t* out,
+                                    const int32_t* ca, const int32_t* cb, int32_t count,
+                                    tfhe_gpu_form form, void* stream);
+/* Batched bootsMUX: out = a ? b : c (cloud.c:11,27). Device batch. */
+tfhe_gpu_status tfhe_gpu_bootsMUX(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* a,
+                                  const int32_t* b, const int32_t* c, int32_t count,
+                                  tfhe_gpu_form form, void* stream);
+/* Host-buffer form of tfhe_gpu_bootsGates: copies in, computes, copies out,
+ * synchronises. `gates` may be NULL with `uniform_gate` used for all. */
+tfhe_gpu_status tfhe_gpu_bootsGates_host(tfhe_gpu_ctx* ctx, const int32_t* gates,
+                                         int32_t uniform_gate, int32_t* out,
+                                         const int32_t* ca, const int32_t* cb,
+                                         int32_t count, tfhe_gpu_form form);
+
+/* ---- client side (host): keygen, encryption, decryption --------------- */
+/* Exact semantics of the reference's numeric functions
+ * (kernel/src/numeric-functions.cpp:11-76, lwe-functions.cpp:21-93) and of
+ * the upstream keyset generation they belong to.  Host-only, no GPU use. */
+
+void tfhe_client_set_seed(const uint32_t* values, int32_t size);
+/* new_random_gate_bootstrapping_secret_keyset: LWE key (n), TLWE key (kN),
+ * key-switching key and time-domain bootstrapping key, in that RNG order. */
+tfhe_gpu_status tfhe_client_gate_keyset(const tfhe_params* params, int32_t* lwe_key,
+                                        int32_t* tlwe_key, int32_t* ks, int32_t* bk);
+/* bootsSymEncrypt of `count` bits into count x (n+1) samples. */
+tfhe_gpu_status tfhe_client_encrypt_bits(const tfhe_params* params, const int32_t* bits,
+                                         int32_t count, const int32_t* lwe_key,
+                                         int32_t* out);
+/* bootsSymDecrypt: bit = phase > 0. */
+tfhe_gpu_status tfhe_client_decrypt_bits(const tfhe_params* params, const int32_t* samples,
+                                         int32_t count, const int32_t* lwe_key,
+                                         int32_t* bits);
+/* phase b - <a, s> of count samples of dimension `dim`. */
+void tfhe_client_phases(const int32_t* samples, int32_t count, int32_t dim,
+                        const int32_t* key, int32_t* phases);
+/* modSwitchToTorus32 (numeric-functions.cpp:71-76). */
+int32_t tfhe_client_mod_switch_to_torus32(int32_t mu, int32_t Msize);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,225 @@
+"""GPU parity of the blind rotation, the bootstrap and the gates against the
+CPU oracle, through the C ABI.
+
+Criteria (the north-star's): every decrypted gate output equals the oracle's
+and the plaintext truth; output phases agree with the oracle's within
+2^-6 of a turn (2^26 units).  Phases cannot agree more tightly in general:
+one rounding difference between two FFT implementations can move a gadget
+digit across its boundary, after which the two accumulators carry different
+masks and independent noise terms (bootstrapping noise ~2^-9 of a turn for
+the default set).  The decision margin is 1/8 of a turn.
+"""
+import numpy as np
+import pytest
+
+from helpers import tlwe_phase, wrap_diff
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+FORMS = ["fp64", "split_fp32"]
+PHASE_TOL = 2 ** 26
+
+
+def dev(torch, x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+def cur(torch):
+    return torch.cuda.current_stream().cuda_stream
+
+
+@pytest.fixture(scope="module")
+def inputs(oracle, keys, P):
+    rng = np.random.default_rng(1)
+    a = rng.integers(0, 2, 64)
+    b = rng.integers(0, 2, 64)
+    oracle.set_seed([1])
+    ca = oracle.encrypt_bits(P, a, keys["lwe"])
+    cb = oracle.encrypt_bits(P, b, keys["lwe"])
+    return a, b, ca, cb
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_blind_rotate_vs_oracle(engine, oracle, keys, torch_cuda, P, inputs, form):
+    torch = torch_cuda
+    _, _, ca, cb = inputs
+    count = 3
+    xs = np.stack([oracle.gate_combine(P, "NAND", ca[i], cb[i]) for i in range(count)])
+    pro = [oracle.bootstrap_prologue(P, 2 ** 29, xs[i]) for i in range(count)]
+    bara = np.stack([p[0] for p in pro])
+    acc0 = np.stack([p[1] for p in pro])
+    d_acc = dev(torch, acc0)
+    engine.tfhe_blindRotate_FFT(d_acc, dev(torch, bara), count, form, stream=cur(torch))
+    torch.cuda.synchronize()
+    got = host(d_acc)
+    for i in range(count):
+        want = oracle.blind_rotate_fft(P, acc0[i], keys["bk_fft"], bara[i])
+        d = wrap_diff(tlwe_phase(got[i], keys["tlwe"], P.N), tlwe_phase(want, keys["tlwe"], P.N))
+        assert np.abs(d).max() <= PHASE_TOL, (form, np.abs(d).max())
+
+
+def test_blind_rotate_zero_steps_is_identity(engine, torch_cuda, P):
+    torch = torch_cuda
+    rng = np.random.default_rng(2)
+    acc = rng.integers(-2 ** 31, 2 ** 31, (2, 2 * P.N)).astype(np.int32)
+    bara = np.zeros((2, P.n), np.int32)
+    for form in FORMS:
+        d_acc = dev(torch, acc)
+        engine.tfhe_blindRotate_FFT(d_acc, dev(torch, bara), 2, form, stream=cur(torch))
+        torch.cuda.synchronize()
+        assert (host(d_acc) == acc).all()
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_bootstrap_wo_ks_vs_oracle(engine, oracle, keys, torch_cuda, P, inputs, form):
+    torch = torch_cuda
+    _, _, ca, cb = inputs
+    count = 4
+    xs = np.stack([oracle.gate_combine(P, "AND", ca[i], cb[i]) for i in range(count)])
+    d_out = torch.zeros((count, P.N + 1), dtype=torch.int32, device="cuda")
+    mu = 2 ** 29
+    engine.tfhe_bootstrap_woKS_FFT(d_out, dev(torch, xs), mu, count, form, stream=cur(torch))
+    torch.cuda.synchronize()
+    got = host(d_out)
+    for i in range(count):
+        want = oracle.bootstrap_woks(P, keys["bk_fft"], mu, xs[i])
+        pg = oracle.phases(got[i], keys["tlwe"], P.N)[0]
+        pw = oracle.phases(want, keys["tlwe"], P.N)[0]
+        assert abs(int(wrap_diff(pg, pw))) <= PHASE_TOL
+        assert np.sign(pg) == np.sign(pw)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("gate", sorted(pyoracle.GATES))
+def test_gate_truth_table(engine, oracle, keys, torch_cuda, P, form, gate):
+    torch = torch_cuda
+    a = np.array([0, 0, 1, 1])
+    b = np.array([0, 1, 0, 1])
+    oracle.set_seed([3])
+    ca = oracle.encrypt_bits(P, a, keys["lwe"])
+    cb = oracle.encrypt_bits(P, b, keys["lwe"])
+    d_out = torch.zeros((4, P.n + 1), dtype=torch.int32, device="cuda")
+    engine.bootsGate(gate, d_out, dev(torch, ca), dev(torch, cb), 4, form, stream=cur(torch))
+    torch.cuda.synchronize()
+    got = oracle.decrypt_bits(P, host(d_out), keys["lwe"])
+    want = np.array([pyoracle.GATE_FN[gate](x, y) for x, y in zip(a, b)])
+    assert (got == want).all()
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_mixed_gates_vs_oracle(engine, oracle, keys, torch_cuda, P, inputs, form):
+    """A mixed batch: same decrypted bits as the oracle and the truth, phases
+    within tolerance of the oracle's."""
+    torch = torch_cuda
+    a, b, ca, cb = inputs
+    count = len(a)
+    rng = np.random.default_rng(4)
+    gates = rng.integers(0, 10, count).astype(np.int32)
+    d_out = torch.zeros((count, P.n + 1), dtype=torch.int32, device="cuda")
+    engine.bootsGates(dev(torch, gates), d_out, dev(torch, ca), dev(torch, cb), count, form,
+                      stream=cur(torch))
+    torch.cuda.synchronize()
+    got = host(d_out)
+    ref = oracle.boots_gate_batch(P, keys["bk_fft"], keys["ks"], gates, ca, cb)
+    names = sorted(pyoracle.GATES, key=lambda g: pyoracle.GATES[g])
+    truth = np.array([pyoracle.GATE_FN[names[g]](x, y) for g, x, y in zip(gates, a, b)])
+    assert (oracle.decrypt_bits(P, got, keys["lwe"]) == truth).all()
+    assert (oracle.decrypt_bits(P, ref, keys["lwe"]) == truth).all()
+    d = wrap_diff(oracle.phases(got, keys["lwe"], P.n), oracle.phases(ref, keys["lwe"], P.n))
+    assert np.abs(d).max() <= PHASE_TOL
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_known_answer_499_or_388(pkg, oracle, torch_cuda, form):
+    """test_bench/ end to end on the GPU, through the host-buffer entry point."""
+    P = pkg.default_params()
+    lwe, tlwe, ks, bk = pkg.gate_keyset(P, [314, 1592, 657])
+    c1 = pkg.encrypt_bits(P, [(499 >> i) & 1 for i in range(16)], lwe)
+    c2 = pkg.encrypt_bits(P, [(388 >> i) & 1 for i in range(16)], lwe)
+    e = pkg.Engine(P)
+    try:
+        e.upload_bootstrapping_key(bk, forms=(form,))
+        e.upload_keyswitch_key(ks)
+        out = e.bootsGates_host(c1, c2, gate="OR", form=form)
+    finally:
+        e.close()
+    bits = pkg.decrypt_bits(P, out, lwe)
+    assert sum(int(x) << i for i, x in enumerate(bits)) == 503
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_mux(engine, oracle, keys, torch_cuda, P, form):
+    torch = torch_cuda
+    combos = np.array([(a, b, c) for a in (0, 1) for b in (0, 1) for c in (0, 1)])
+    oracle.set_seed([5])
+    enc = [oracle.encrypt_bits(P, combos[:, i], keys["lwe"]) for i in range(3)]
+    d_out = torch.zeros((8, P.n + 1), dtype=torch.int32, device="cuda")
+    engine.bootsMUX(d_out, dev(torch, enc[0]), dev(torch, enc[1]), dev(torch, enc[2]), 8, form,
+                    stream=cur(torch))
+    torch.cuda.synchronize()
+    got = oracle.decrypt_bits(P, host(d_out), keys["lwe"])
+    want = np.where(combos[:, 0] == 1, combos[:, 1], combos[:, 2])
+    assert (got == want).all()
+    ref = np.stack([oracle.boots_mux(P, keys["bk_fft"], keys["ks"], enc[0][i], enc[1][i], enc[2][i])
+                    for i in range(2)])
+    d = wrap_diff(oracle.phases(host(d_out)[:2], keys["lwe"], P.n), oracle.phases(ref, keys["lwe"], P.n))
+    assert np.abs(d).max() <= PHASE_TOL
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_large_batch_no_failures(engine, pkg, keys, torch_cuda, P, form):
+    """4096 random gates in one call (the batched circuit-layer size): every
+    output decrypts to the truth; output noise well inside the margin."""
+    torch = torch_cuda
+    rng = np.random.default_rng(6)
+    count = 4096
+    a = rng.integers(0, 2, count)
+    b = rng.integers(0, 2, count)
+    gates = rng.integers(0, 10, count).astype(np.int32)
+    pkg.set_seed([6])
+    ca = pkg.encrypt_bits(pkg.default_params(), a, keys["lwe"])
+    cb = pkg.encrypt_bits(pkg.default_params(), b, keys["lwe"])
+    d_out = torch.zeros((count, P.n + 1), dtype=torch.int32, device="cuda")
+    engine.bootsGates(dev(torch, gates), d_out, dev(torch, ca), dev(torch, cb), count, form,
+                      stream=cur(torch))
+    torch.cuda.synchronize()
+    out = host(d_out)
+    names = sorted(pyoracle.GATES, key=lambda g: pyoracle.GATES[g])
+    truth = np.array([pyoracle.GATE_FN[names[g]](x, y) for g, x, y in zip(gates, a, b)])
+    got = pkg.decrypt_bits(pkg.default_params(), out, keys["lwe"])
+    assert (got == truth).all()
+    ph = pkg.phases(out, keys["lwe"]).astype(np.int64)
+    err = np.abs(np.abs(ph) - 2 ** 29)
+    print("%s: output |phase - mu| max 2^%.2f mean 2^%.2f of a turn"
+          % (form, np.log2(err.max()) - 32, np.log2(err.mean()) - 32))
+    assert err.max() < 2 ** 28  # under 1/16 of a turn
+
+
+def test_errors_are_status_codes(pkg, keys, torch_cuda, P):
+    torch = torch_cuda
+    e = pkg.Engine(pkg.default_params())
+    try:
+        d = torch.zeros((1, P.n + 1), dtype=torch.int32, device="cuda")
+        with pytest.raises(pkg.TfheError) as ei:
+            e.bootsGate("NAND", d, d, d, 1, "fp64")
+        assert ei.value.status == 5  # NO_KEY
+        e.upload_bootstrapping_key(keys["bk"], forms=("fp64",))
+        with pytest.raises(pkg.TfheError) as ei:
+            e.bootsGate("NAND", d, d, d, 1, "fp64")  # KS key missing
+        assert ei.value.status == 5
+        with pytest.raises(pkg.TfheError) as ei:
+            e.bootsGate("NAND", d, d, d, 1, "split_fp32")  # form not built
+        assert ei.value.status == 5
+        with pytest.raises(pkg.TfheError) as ei:
+            e.bootsGate("NAND", d, d, d, 1, 7)
+        assert ei.value.status == 1
+        e.upload_keyswitch_key(keys["ks"])
+        e.bootsGate("NAND", d, d, d, 0, "fp64")  # empty batch is a no-op
+        e.synchronize()
+    finally:
+        e.close()
