@@ -1,0 +1,398 @@
+"""Benchmark: gate bootstraps/sec on one GB300 (batched circuit layer).
+
+Workload (one "step"): a circuit layer of 4096 independent gate bootstraps,
+mixed NAND/AND/XOR/OR drawn uniformly from a seed, default 110-bit parameter
+set (n=630, N=1024, k=1, l=3, Bgbit=7, t=8, basebit=2), one cloud key from
+seed 0, input bits from seed 4.  Synthetic data: no dataset is involved.
+
+  value  -- bootstraps/s of the split-FP32 form with inputs resident in HBM,
+            timed with CUDA events around each step on the launching stream,
+            L2 flushed (a 256 MB write) between steps outside the timed
+            intervals; max over ranks.
+  e2e    -- the same metric through the host-buffer C entry point
+            (tfhe_gpu_bootsGates_host): pinned host ciphertexts in, results
+            out, copies inside the timed region.
+  roofline -- the dominant kernel (the blind-rotation kernel,
+            k_external_product<float,2,BlindRotate>) timed alone with CUDA
+            events: algorithmic FP work 162.6 MFLOP per bootstrap (FFT-form
+            count) over its duration, against the FP32 pipe peak.
+  cpu_baseline -- the CPU oracle (restated reference path) on the host's
+            cores on a bounded sample.
+
+`--impl reference` times the reference's CPU path instead (the oracle
+restatement; the upstream library the reference links is not available) and
+prints the same line with "impl": "reference".
+
+Multi-GPU (torchrun): each rank runs an independent replica of the step on
+its own GPU (gate bootstraps of a layer are independent); value = all ranks'
+bootstraps / max rank time; "scaling": "weak".
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOP_PER_BOOTSTRAP = 162.6e6      # FFT-form algorithmic count, default set
+BATCH = 4096
+GATE_SET = (0, 1, 3, 2)           # NAND, AND, XOR, OR
+L2_FLUSH_BYTES = 256 << 20
+SMS = 152
+FP32_LANES_PER_SM = 128
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--form", default="split_fp32", choices=["split_fp32", "fp64"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the FP64 / single-gate / CPU side measurements")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_inputs(pkg, P, lwe_key, batch, seed=4):
+    rng = np.random.default_rng(seed)
+    a = rng.integers(0, 2, batch)
+    b = rng.integers(0, 2, batch)
+    gates = np.array(GATE_SET, np.int32)[rng.integers(0, len(GATE_SET), batch)]
+    pkg.set_seed([seed])
+    ca = pkg.encrypt_bits(P, a, lwe_key)
+    cb = pkg.encrypt_bits(P, b, lwe_key)
+    return a, b, gates, ca, cb
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock / throttle reasons during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(seconds, batch_hint):
+    """The oracle (restated reference path) on all host cores, bounded."""
+    from oracle import pyoracle
+    import __graft_entry__ as ge  # noqa: F401
+    o = pyoracle.get()
+    P = pyoracle.default_params()
+    lwe, tlwe, ks, bk = o.gate_keyset(P, [0])
+    bk_fft = o.bk_to_fft(P, bk)
+    threads = o.max_threads()
+    rng = np.random.default_rng(4)
+    n = max(threads, 1) * 2
+    a = rng.integers(0, 2, n)
+    b = rng.integers(0, 2, n)
+    gates = np.array(GATE_SET, np.int32)[rng.integers(0, len(GATE_SET), n)]
+    o.set_seed([4])
+    ca = o.encrypt_bits(P, a, lwe)
+    cb = o.encrypt_bits(P, b, lwe)
+    done = 0
+    t0 = time.perf_counter()
+    while True:
+        o.boots_gate_batch(P, bk_fft, ks, gates, ca, cb, threads)
+        done += n
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return {"value": done / el, "unit": "bootstraps/s", "cores": threads, "kind": "port",
+            "sample": "%d gate bootstraps (mixed NAND/AND/XOR/OR, default set) in %.1f s on %d threads"
+                      % (done, el, threads)}
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the reference's CPU path (restated) on host cores."""
+    if world > 1 and rank != 0:
+        return
+    from oracle import pyoracle
+    o = pyoracle.get()
+    P = pyoracle.default_params()
+    lwe, tlwe, ks, bk = o.gate_keyset(P, [0])
+    bk_fft = o.bk_to_fft(P, bk)
+    threads = o.max_threads()
+    n = max(2 * threads, 8)  # bounded sample of the 4096-gate layer per step
+    rng = np.random.default_rng(4)
+    a = rng.integers(0, 2, n)
+    b = rng.integers(0, 2, n)
+    gates = np.array(GATE_SET, np.int32)[rng.integers(0, len(GATE_SET), n)]
+    o.set_seed([4])
+    ca = o.encrypt_bits(P, a, lwe)
+    cb = o.encrypt_bits(P, b, lwe)
+    for _ in range(args.warmup):
+        o.boots_gate_batch(P, bk_fft, ks, gates, ca, cb, threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.boots_gate_batch(P, bk_fft, ks, gates, ca, cb, threads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = n * args.steps / total
+    line = {
+        "metric": "gate bootstraps/sec", "value": value, "unit": "bootstraps/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "batched circuit layer of mixed NAND/AND/XOR/OR gate bootstraps, "
+                               "default 110-bit set (n=630, N=1024, k=1, l=3, Bgbit=7, t=8, basebit=2); "
+                               "each step a bounded sample of %d gates of the 4096-gate layer" % n,
+                   "batch": n, "form": "fp64 (2N-point FFT restatement)"},
+        "cpu_baseline": {"value": value, "unit": "bootstraps/s", "cores": threads, "kind": "port",
+                         "sample": "%d gates per step x %d steps" % (n, args.steps)},
+        "e2e": {"value": value, "unit": "bootstraps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    import torch
+    import __graft_entry__ as ge
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    ge.build()
+    pkg = ge.load_package()
+    P = pkg.default_params()
+    lwe, tlwe, ks, bk = pkg.gate_keyset(P, [0])
+    eng = pkg.Engine(P, device=local)
+    eng.upload_bootstrapping_key(bk, forms=("fp64", "split_fp32"))
+    eng.upload_keyswitch_key(ks)
+    batch = args.batch
+    a, b, gates, ca, cb = make_inputs(pkg, P, lwe, batch)
+    dev = torch.device("cuda", local)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    # a non-default stream: the engine maps a NULL stream to its own stream,
+    # so events must be recorded on the stream the engine launches on
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    sp = stream.cuda_stream
+    assert sp, "need a non-null stream handle"
+    d_ca = torch.from_numpy(ca).to(dev)
+    d_cb = torch.from_numpy(cb).to(dev)
+    d_g = torch.from_numpy(gates).to(dev)
+    d_out = torch.empty_like(d_ca)
+    torch.cuda.synchronize()
+
+    def step(form):
+        eng.bootsGates(d_g, d_out, d_ca, d_cb, batch, form, stream=sp)
+
+    # warm-up (also sizes the engine's scratch)
+    for _ in range(args.warmup):
+        step(args.form)
+    torch.cuda.synchronize()
+
+    def timed(form, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        for s in range(steps):
+            flush.fill_(s)  # evict L2 between steps (outside the timed interval)
+            evs[s][0].record(stream)
+            step(form)
+            evs[s][1].record(stream)
+        torch.cuda.synchronize()
+        return [e0.elapsed_time(e1) for e0, e1 in evs]
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = timed(args.form, args.steps)
+    torch.cuda.synchronize()
+    total_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * batch * args.steps / (total_ms / 1000.0)
+    truth = {0: lambda x, y: 1 - (x & y), 1: lambda x, y: x & y, 2: lambda x, y: x | y,
+             3: lambda x, y: x ^ y}
+    d_out.zero_()
+    step(args.form)
+    torch.cuda.synchronize()
+    out = d_out.cpu().numpy()
+    ok = bool((pkg.decrypt_bits(P, out, lwe)
+               == np.array([truth[int(g)](x, y) for g, x, y in zip(gates, a, b)])).all())
+
+    # e2e through the host-buffer entry point (pinned host buffers)
+    h_ca = torch.from_numpy(ca).pin_memory()
+    h_cb = torch.from_numpy(cb).pin_memory()
+    h_g = torch.from_numpy(gates).pin_memory()
+    h_out = torch.empty_like(h_ca).pin_memory()
+    lib = pkg.lib()
+    e2e_ms = []
+    for s in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = lib.tfhe_gpu_bootsGates_host(
+            eng.ctx, pkg.ctypes.cast(h_g.data_ptr(), pkg.I32P), 0,
+            pkg.ctypes.cast(h_out.data_ptr(), pkg.I32P), pkg.ctypes.cast(h_ca.data_ptr(), pkg.I32P),
+            pkg.ctypes.cast(h_cb.data_ptr(), pkg.I32P), batch, pkg.FORMS[args.form])
+        if st:
+            raise RuntimeError("bootsGates_host failed: %d" % st)
+        if s >= args.warmup:
+            e2e_ms.append(1000 * (time.perf_counter() - t0))
+    e2e_total = sum(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = world * batch * args.steps / (e2e_total / 1000.0)
+    lwe_bytes = batch * (P.n + 1) * 4
+
+    # dominant kernel alone: blind rotation + extraction on resident inputs
+    x = torch.empty_like(d_ca)
+    u = torch.empty((batch, P.k * P.N + 1), dtype=torch.int32, device=dev)
+    lib.tfhe_gpu_bootsGate  # noqa: B018  (ensure symbol)
+    kms = []
+    for s in range(max(3, args.steps)):
+        flush.fill_(s)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.tfhe_bootstrap_woKS_FFT(u, d_ca, 2 ** 29, batch, args.form, stream=sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        kms.append(e0.elapsed_time(e1))
+    k_ms = statistics.median(kms)
+    achieved = FLOP_PER_BOOTSTRAP * batch / (k_ms / 1000.0) / 1e12
+    clocks = clk.summary()
+    sm_max = clocks.get("sm_max_mhz") or 2070.0
+    peak = SMS * FP32_LANES_PER_SM * 2 * sm_max * 1e6 / 1e12
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # plain FP64 form, same batch
+        for _ in range(1):
+            step("fp64")
+        torch.cuda.synchronize()
+        f64 = timed("fp64", 2)
+        extras["fp64_batched_bootstraps_per_s"] = batch * 2 / (sum(f64) / 1000.0)
+        # plain FP64 single-gate form (one gate per call), the >=10x denominator
+        one_ms = []
+        for s in range(4):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.bootsGates(d_g, d_out, d_ca, d_cb, 1, "fp64", stream=sp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            one_ms.append(e0.elapsed_time(e1))
+        one = statistics.median(one_ms[1:])
+        extras["fp64_single_gate_ms"] = one
+        extras["fp64_single_gate_bootstraps_per_s"] = 1000.0 / one
+        extras["speedup_vs_fp64_single_gate"] = value / world / (1000.0 / one)
+        cpu = cpu_baseline(args.cpu_seconds, batch)
+    else:
+        cpu = None
+
+    if rank == 0:
+        p50 = statistics.median(ms)
+        p99 = float(np.percentile(ms, 99))
+        line = {
+            "metric": "gate bootstraps/sec", "value": value, "unit": "bootstraps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.form == "split_fp32" else "f64",
+            "data": "synthetic",
+            "config": {"workload": "batched circuit layer: %d independent gate bootstraps, mixed "
+                                   "NAND/AND/XOR/OR (seed 4), default 110-bit set (n=630, N=1024, k=1, "
+                                   "l=3, Bgbit=7, t=8, basebit=2), one cloud key (seed 0)" % batch,
+                       "batch": batch, "form": args.form, "split_bits": eng.params.split_bits,
+                       "l2": "flushed (256 MB write) between timed steps", "parallelism": "replicas"},
+            "latency_ms": {"p50": p50, "p99": p99,
+                           "note": "per-gate latency = completion time of its batch"},
+            "decrypt_ok": ok,
+            "e2e": {"value": e2e_value, "unit": "bootstraps/s",
+                    "h2d_bytes_per_step": 2 * lwe_bytes + batch * 4, "d2h_bytes_per_step": lwe_bytes},
+            "gpu_launches": 3 * args.steps,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "k_external_product<float,2,BlindRotate> (blind rotation + extraction)",
+                         "kernel_ms": k_ms,
+                         "peak_source": "nominal FP32 pipe: 152 SMs x 128 lanes x 2 x max SM clock "
+                                        "(no measured FP32 peak in MEASURED_PEAKS.json)"},
+            "clocks": clocks,
+        }
+        line.update(extras)
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

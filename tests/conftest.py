@@ -52,6 +52,10 @@ def torch_cuda():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
+    # Work on a non-default stream: torch's copies and the engine's launches
+    # (given this stream's handle) are then ordered on one stream.  A NULL
+    # handle would send the engine's work to its own stream instead.
+    torch.cuda.set_stream(torch.cuda.Stream())
     return torch
 
 
