@@ -107,6 +107,8 @@ SIGNATURES = {
     "tfhe_gpu_bootsMUX": (ctypes.c_int, [VP, VP, VP, VP, VP, ctypes.c_int32, ctypes.c_int, VP]),
     "tfhe_gpu_bootsGates_host": (ctypes.c_int, [VP, I32P, ctypes.c_int32, I32P, I32P, I32P,
                                                 ctypes.c_int32, ctypes.c_int]),
+    "tfhe_gpu_bootsGates_noalloc": (ctypes.c_int, [VP, VP, VP, VP, VP, ctypes.c_int32, ctypes.c_int,
+                                                   VP]),
     "tfhe_client_set_seed": (None, [U32P, ctypes.c_int32]),
     "tfhe_client_gate_keyset": (ctypes.c_int, [ctypes.c_void_p, I32P, I32P, I32P, I32P]),
     "tfhe_client_encrypt_bits": (ctypes.c_int, [ctypes.c_void_p, I32P, ctypes.c_int32, I32P, I32P]),
@@ -342,6 +344,14 @@ class Engine:
     def bootsGates(self, gates, out, ca, cb, count, form, stream=None):
         self._check(self.lib.tfhe_gpu_bootsGates(self.ctx, _ptr(gates), _ptr(out), _ptr(ca), _ptr(cb),
                                                  count, self._form(form), stream), "bootsGates")
+
+    def bootsGates_noalloc(self, gates, out, ca, cb, count, form, stream=None):
+        """tfhe_gpu_bootsGates without any allocation inside the call (fixed
+        device scratch in the library; up to 512 gates of the default set;
+        calls overlapping on the GPU must be serialised)."""
+        self._check(self.lib.tfhe_gpu_bootsGates_noalloc(self.ctx, _ptr(gates), _ptr(out), _ptr(ca),
+                                                         _ptr(cb), count, self._form(form), stream),
+                    "bootsGates_noalloc")
 
     def bootsMUX(self, out, a, b, c, count, form, stream=None):
         self._check(self.lib.tfhe_gpu_bootsMUX(self.ctx, _ptr(out), _ptr(a), _ptr(b), _ptr(c), count,

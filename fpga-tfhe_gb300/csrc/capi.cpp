@@ -14,27 +14,10 @@
 #include <vector>
 
 #include "../../include/tfhe_gpu.h"
+#include "ctx.h"
 #include "engine.h"
 
 using namespace tfhe_gb300;
-
-struct tfhe_gpu_ctx {
-    tfhe_params P;
-    DevParams dp;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    void* d_tables = nullptr;  // 1024 double2 then 1024 float2
-    Tables tables{};
-    void* d_bk[kNumForms] = {nullptr, nullptr};
-    int32_t* d_ks = nullptr;
-    int32_t ks_row_stride = 0;
-    // scratch slots, grown on demand
-    void* d_scratch[4] = {nullptr, nullptr, nullptr, nullptr};
-    size_t scratch_bytes[4] = {0, 0, 0, 0};
-    int groups_per_cta[kNumForms] = {4, 4};
-    std::string last_error;
-    size_t key_bytes = 0;
-};
 
 namespace {
 

@@ -1,0 +1,32 @@
+// ctx.h -- the engine context behind the opaque tfhe_gpu_ctx handle of the
+// C ABI (include/tfhe_gpu.h).  Internal: only the engine's own translation
+// units include it.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/tfhe_gpu.h"
+#include "engine.h"
+
+using tfhe_gb300::DevParams;
+using tfhe_gb300::kNumForms;
+using tfhe_gb300::Tables;
+
+struct tfhe_gpu_ctx {
+    tfhe_params P;
+    DevParams dp;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void* d_tables = nullptr;  // 1024 double2 then 1024 float2
+    Tables tables{};
+    void* d_bk[kNumForms] = {nullptr, nullptr};
+    int32_t* d_ks = nullptr;
+    int32_t ks_row_stride = 0;
+    // scratch slots, grown on demand
+    void* d_scratch[4] = {nullptr, nullptr, nullptr, nullptr};
+    size_t scratch_bytes[4] = {0, 0, 0, 0};
+    int groups_per_cta[kNumForms] = {4, 4};
+    std::string last_error;
+    size_t key_bytes = 0;
+};

@@ -212,6 +212,21 @@ tfhe_gpu_status tfhe_gpu_bootsGates_host(tfhe_gpu_ctx* ctx, const int32_t* gates
                                          const int32_t* ca, const int32_t* cb,
                                          int32_t count, tfhe_gpu_form form);
 
+/* Same result as tfhe_gpu_bootsGates, but the call allocates no memory: its
+ * intermediate samples live in a fixed 3.4 MB device array built into the
+ * library (held on every GPU that loads it), for callers that must not
+ * allocate inside a call (fixed memory budgets, latency-critical loops where
+ * cudaMalloc/cudaFree would synchronise the device, frameworks that own all
+ * device memory).  No counterpart in the reference.  Limit: count x
+ * (n + 1 + kN + 1) int32 words <= 847,872 (512 gates of the default set);
+ * larger calls return TFHE_GPU_BAD_PARAM.  The first call on a device looks
+ * up the array's address (make it before any stream capture).  Calls that
+ * overlap on the GPU share the array and race: serialise them. */
+tfhe_gpu_status tfhe_gpu_bootsGates_noalloc(tfhe_gpu_ctx* ctx, const int32_t* gates,
+                                            int32_t* out, const int32_t* ca,
+                                            const int32_t* cb, int32_t count,
+                                            tfhe_gpu_form form, void* stream);
+
 /* ---- client side (host): keygen, encryption, decryption --------------- */
 /* Exact semantics of the reference's numeric functions
  * (kernel/src/numeric-functions.cpp:11-76, lwe-functions.cpp:21-93) and of
