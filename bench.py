@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--form", default="split_fp32", choices=["split_fp32", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--groups", type=int, default=0,
+                    help="ciphertexts per CTA of the split-FP32 blind rotation (0 = engine default)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64 / single-gate / CPU side measurements")
     return ap.parse_args()
@@ -229,6 +231,8 @@ def main():
     eng = pkg.Engine(P, device=local)
     eng.upload_bootstrapping_key(bk, forms=("fp64", "split_fp32"))
     eng.upload_keyswitch_key(ks)
+    if args.groups:
+        eng.set_groups_per_cta("split_fp32", args.groups)
     batch = args.batch
     a, b, gates, ca, cb = make_inputs(pkg, P, lwe, batch)
     dev = torch.device("cuda", local)
@@ -370,6 +374,7 @@ def main():
                                    "NAND/AND/XOR/OR (seed 4), default 110-bit set (n=630, N=1024, k=1, "
                                    "l=3, Bgbit=7, t=8, basebit=2), one cloud key (seed 0)" % batch,
                        "batch": batch, "form": args.form, "split_bits": eng.params.split_bits,
+                       "groups_per_cta": eng.get_groups_per_cta(args.form),
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": "replicas"},
             "latency_ms": {"p50": p50, "p99": p99,
                            "note": "per-gate latency = completion time of its batch"},

@@ -81,6 +81,8 @@ SIGNATURES = {
     "tfhe_gpu_synchronize": (ctypes.c_int, [VP]),
     "tfhe_gpu_tgsw_fft_bytes": (ctypes.c_size_t, [VP, ctypes.c_int]),
     "tfhe_gpu_device_bytes": (ctypes.c_size_t, [VP]),
+    "tfhe_gpu_set_groups_per_cta": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int32]),
+    "tfhe_gpu_get_groups_per_cta": (ctypes.c_int32, [VP, ctypes.c_int]),
     "tfhe_gpu_upload_bootstrapping_key": (ctypes.c_int, [VP, I32P, ctypes.c_uint32]),
     "tfhe_gpu_upload_bootstrapping_key_fft": (ctypes.c_int, [VP, F64P, ctypes.c_uint32]),
     "tfhe_gpu_upload_keyswitch_key": (ctypes.c_int, [VP, I32P]),
@@ -252,6 +254,13 @@ class Engine:
 
     def device_bytes(self):
         return self.lib.tfhe_gpu_device_bytes(self.ctx)
+
+    def set_groups_per_cta(self, form, groups):
+        self._check(self.lib.tfhe_gpu_set_groups_per_cta(self.ctx, self._form(form), int(groups)),
+                    "set_groups_per_cta")
+
+    def get_groups_per_cta(self, form):
+        return self.lib.tfhe_gpu_get_groups_per_cta(self.ctx, self._form(form))
 
     # keys
     def upload_bootstrapping_key(self, bk, forms=("fp64", "split_fp32")):

@@ -23,6 +23,7 @@
 //   X^{2N-b} rotation            kernel/src/tfhe_blindRotateAndExtract/mulByXaiOrCopy.cpp:25-41
 #include <math.h>
 
+#include "async_copy.cuh"
 #include "engine.h"
 #include "fft512.cuh"
 
@@ -32,6 +33,12 @@ namespace {
 
 constexpr int kN = 1024;
 constexpr int kHalf = 512;
+// Table layout (complex entries): W^(tq) as [q][t] (512), W^(8jq) as [q][j]
+// (64), then psi^x (512).
+constexpr int kTabA = 0;
+constexpr int kTabB = 512;
+constexpr int kTabPsi = 576;
+constexpr int kTabSize = 1088;
 
 // ----------------------------------------------------------------------
 // helpers
@@ -76,49 +83,110 @@ __device__ __forceinline__ int64_t to_int<float>(float v) {
 
 // ----------------------------------------------------------------------
 // shared-memory plan of the FFT kernels
-//   [tables: 1024 cpx<R>] then per 64-thread group:
-//   [acc: 2 x 1024 int32][scratch: 4 x 576 R]
+//   [tables: kTabSize cpx<R>] then per 64-thread group:
+//   [acc: 2 x 1024 int32][NB x 2 exchange buffers of 576 cpx<R>]
+// NB = number of transforms run together (max of L and the parts).
 // ----------------------------------------------------------------------
-template <typename R>
+template <typename R, int NB>
 struct SmemPlan {
-    static constexpr size_t tables = 1024 * sizeof(cpx<R>);
+    static constexpr size_t tables = kTabSize * sizeof(cpx<R>);
     static constexpr size_t acc = 2 * kN * sizeof(int32_t);
-    static constexpr size_t scratch = 4 * kScratchStride * sizeof(R);
+    static constexpr size_t scratch = NB * 2 * kScratchStride * sizeof(cpx<R>);
     static constexpr size_t group = acc + scratch;
     static size_t total(int groups) { return tables + groups * group; }
 };
 
 template <typename R>
 __device__ __forceinline__ FftScratch<R> scratch_at(char* base) {
-    R* s = reinterpret_cast<R*>(base);
-    return {s, s + kScratchStride, s + 2 * kScratchStride, s + 3 * kScratchStride};
+    cpx<R>* s = reinterpret_cast<cpx<R>*>(base);
+    return {s, s + kScratchStride};
 }
 
 template <typename R>
 __device__ __forceinline__ void load_tables(cpx<R>* dst, const Tables& T) {
     const cpx<R>* src = table_ptr<R>(T);
-    for (int i = threadIdx.x; i < 1024; i += blockDim.x) dst[i] = src[i];
+    for (int i = threadIdx.x; i < kTabSize; i += blockDim.x) dst[i] = src[i];
+}
+
+template <typename R>
+__device__ __forceinline__ FftTwiddles<R> twiddles_at(const cpx<R>* tables) {
+    return {tables + kTabA, tables + kTabB};
 }
 
 // ----------------------------------------------------------------------
 // the fused step: out = EP(ROT ? (X^a - 1) acc : acc);
 //                 acc = (ROT ? acc : 0) + out
-// gsw: one TGSW in engine layout [kpl][2][PARTS][512 key_index order].
+// A key row p of a TGSW in engine layout is [2 outputs][PARTS][512
+// key_index order] complex values; `Keys` says where rows come from:
+//   GlobalKeys -- straight from global memory (L2), 16-byte loads, with an
+//                 L1 prefetch of the rows ahead of the transform;
+//   RingKeys   -- from a shared-memory ring filled by a producer warp with
+//                 bulk copies (see k_blind_rotate_ring).
+// FB digit polynomials are transformed together (fft512_forward_multi), and
+// IB parts of an output polynomial are transformed back together.
 // ----------------------------------------------------------------------
-template <typename R, int PARTS>
+template <typename R, int PARTS, int NB>
 struct StepCtx {
-    const cpx<R>* tw;   // smem W_512^k
+    FftTwiddles<R> tw;  // smem W_512 powers, per pass
     const cpx<R>* psi;  // smem psi^x
-    FftScratch<R> s;
+    FftScratch<R> s[NB];
     int32_t* acc;       // smem 2 x N
     int t, bar_id;
-    int l, Bgbit, split;
+    int Bgbit, split;
     uint32_t offset;
 };
 
-template <typename R, int PARTS, bool ROT>
-__device__ __forceinline__ void ep_step(const StepCtx<R, PARTS>& S,
-                                        const cpx<R>* __restrict__ gsw, int a) {
+template <typename R, int PARTS>
+struct GlobalKeys {
+    static constexpr size_t kRow = (size_t)2 * PARTS * kHalf;
+    const cpx<R>* gsw;
+    __device__ __forceinline__ void prefetch(int p0, int np, int t) const {
+        const int lines = (int)(np * kRow * sizeof(cpx<R>) / 128);
+        const char* gb = reinterpret_cast<const char*>(gsw + (size_t)p0 * kRow);
+        for (int ln = t; ln < lines; ln += 64)
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(gb + (size_t)ln * 128));
+    }
+    __device__ __forceinline__ const cpx<R>* acquire(int p) const { return gsw + (size_t)p * kRow; }
+    __device__ __forceinline__ void release(int) const {}
+    static constexpr bool kShared = false;
+};
+
+template <bool SHARED>
+__device__ __forceinline__ float4 key_load4(const float4* p) {
+    if constexpr (SHARED) return *p;
+    else return __ldg(p);
+}
+
+template <typename R, int PARTS, bool SHARED>
+__device__ __forceinline__ void mac_row(cpx<R> (&out)[2][PARTS][8], const cpx<R> (&v)[8],
+                                        const cpx<R>* __restrict__ g, int t) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int pt = 0; pt < PARTS; ++pt) {
+            const cpx<R>* gk = g + (j * PARTS + pt) * kHalf;
+            if constexpr (sizeof(R) == 4) {
+                const float4* g4 = reinterpret_cast<const float4*>(gk);
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) {
+                    const float4 w = key_load4<SHARED>(g4 + qq * 64 + t);
+                    const cpx<R> k0 = {(R)w.x, (R)w.y}, k1 = {(R)w.z, (R)w.w};
+                    out[j][pt][2 * qq] = cadd(out[j][pt][2 * qq], cmul(v[2 * qq], k0));
+                    out[j][pt][2 * qq + 1] = cadd(out[j][pt][2 * qq + 1], cmul(v[2 * qq + 1], k1));
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const cpx<R> k0 = gk[key_index<R>(t, q)];
+                    out[j][pt][q] = cadd(out[j][pt][q], cmul(v[q], k0));
+                }
+            }
+        }
+}
+
+template <typename R, int PARTS, bool ROT, int L, int FB, int IB, int NB, typename Keys>
+__device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, const Keys& keys, int a) {
+    static_assert(L % FB == 0 && PARTS % IB == 0 && FB <= NB && IB <= NB, "batch sizes");
     const int t = S.t;
     const int halfBg = 1 << (S.Bgbit - 1);
     const uint32_t mask = (1u << S.Bgbit) - 1;
@@ -131,7 +199,9 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS>& S,
 #pragma unroll
             for (int q = 0; q < 8; ++q) out[j][pt][q] = {(R)0, (R)0};
 
+#pragma unroll 1
     for (int jp = 0; jp < 2; ++jp) {
+        keys.prefetch(jp * L, L, t);
         const int32_t* src = S.acc + jp * kN;
         uint32_t r0[8], r1[8];
 #pragma unroll
@@ -147,69 +217,64 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS>& S,
             r0[r] += S.offset;
             r1[r] += S.offset;
         }
-        for (int lev = 0; lev < S.l; ++lev) {
-            const int p = jp * S.l + lev;
-            const int decal = 32 - (lev + 1) * S.Bgbit;
-            cpx<R> v[8];
+#pragma unroll
+        for (int lev0 = 0; lev0 < L; lev0 += FB) {
+            cpx<R> v[FB][8];
 #pragma unroll
             for (int r = 0; r < 8; ++r) {
-                const int d0 = (int)((r0[r] >> decal) & mask) - halfBg;
-                const int d1 = (int)((r1[r] >> decal) & mask) - halfBg;
-                v[r] = cmul(cpx<R>{(R)d0, (R)d1}, S.psi[t + 64 * r]);
-            }
-            fft512_forward(v, S.s, S.tw, t, S.bar_id);
-            const cpx<R>* g = gsw + (size_t)p * 2 * PARTS * kHalf;
+                const cpx<R> ps = S.psi[t + 64 * r];
 #pragma unroll
-            for (int j = 0; j < 2; ++j)
-#pragma unroll
-                for (int pt = 0; pt < PARTS; ++pt) {
-                    const cpx<R>* gk = g + (j * PARTS + pt) * kHalf;
-                    if constexpr (sizeof(R) == 4) {
-                        const float4* g4 = reinterpret_cast<const float4*>(gk);
-#pragma unroll
-                        for (int qq = 0; qq < 4; ++qq) {
-                            const float4 w = __ldg(g4 + qq * 64 + t);
-                            const cpx<R> k0 = {(R)w.x, (R)w.y}, k1 = {(R)w.z, (R)w.w};
-                            out[j][pt][2 * qq] = cadd(out[j][pt][2 * qq], cmul(v[2 * qq], k0));
-                            out[j][pt][2 * qq + 1] =
-                                cadd(out[j][pt][2 * qq + 1], cmul(v[2 * qq + 1], k1));
-                        }
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) {
-                            const cpx<R> k0 = gk[key_index<R>(t, q)];
-                            out[j][pt][q] = cadd(out[j][pt][q], cmul(v[q], k0));
-                        }
-                    }
+                for (int b = 0; b < FB; ++b) {
+                    const int decal = 32 - (lev0 + b + 1) * S.Bgbit;
+                    const int d0 = (int)((r0[r] >> decal) & mask) - halfBg;
+                    const int d1 = (int)((r1[r] >> decal) & mask) - halfBg;
+                    v[b][r] = cmul(cpx<R>{(R)d0, (R)d1}, ps);
                 }
+            }
+            fft512_forward_multi<FB>(v, *reinterpret_cast<const FftScratch<R>(*)[FB]>(S.s), S.tw, t,
+                                     S.bar_id);
+#pragma unroll
+            for (int b = 0; b < FB; ++b) {
+                const int p = jp * L + lev0 + b;
+                mac_row<R, PARTS, Keys::kShared>(out, v[b], keys.acquire(p), t);
+                keys.release(p);
+            }
         }
     }
 
-    // back to the coefficient domain, one output polynomial at a time
+    // back to the coefficient domain (j unrolled: out[j] must stay in registers)
     const R inv = (R)(1.0 / 512.0);
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
         uint32_t c0[8], c1[8];
 #pragma unroll
-        for (int pt = 0; pt < PARTS; ++pt) {
-            cpx<R> v[8];
+        for (int pt0 = 0; pt0 < PARTS; pt0 += IB) {
+            cpx<R> v[IB][8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) v[q] = out[j][pt][q];
-            fft512_inverse(v, S.s, S.tw, t, S.bar_id);
+            for (int b = 0; b < IB; ++b)
+#pragma unroll
+                for (int q = 0; q < 8; ++q) v[b][q] = out[j][pt0 + b][q];
+            fft512_inverse_multi<IB>(v, *reinterpret_cast<const FftScratch<R>(*)[IB]>(S.s), S.tw, t,
+                                     S.bar_id);
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                cpx<R> z = cmulc(v[q], S.psi[t + 64 * q]);
-                const uint32_t a0 = (uint32_t)(uint64_t)to_int<R>(z.x * inv);
-                const uint32_t a1 = (uint32_t)(uint64_t)to_int<R>(z.y * inv);
-                if (PARTS == 1) {
-                    c0[q] = a0;
-                    c1[q] = a1;
-                } else if (pt == 0) {  // high part, scaled by 2^split
-                    c0[q] = a0 << S.split;
-                    c1[q] = a1 << S.split;
-                } else {
-                    c0[q] += a0;
-                    c1[q] += a1;
+                const cpx<R> ps = S.psi[t + 64 * q];
+#pragma unroll
+                for (int b = 0; b < IB; ++b) {
+                    const int pt = pt0 + b;
+                    const cpx<R> z = cmulc(v[b][q], ps);
+                    const uint32_t a0 = (uint32_t)(uint64_t)to_int<R>(z.x * inv);
+                    const uint32_t a1 = (uint32_t)(uint64_t)to_int<R>(z.y * inv);
+                    if (PARTS == 1) {
+                        c0[q] = a0;
+                        c1[q] = a1;
+                    } else if (pt == 0) {  // high part, scaled by 2^split
+                        c0[q] = a0 << S.split;
+                        c1[q] = a1 << S.split;
+                    } else {
+                        c0[q] += a0;
+                        c1[q] += a1;
+                    }
                 }
             }
         }
@@ -230,12 +295,15 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS>& S,
 }
 
 struct KParams {
-    int n, l, Bgbit, split;
+    int n, Bgbit, split;
     uint32_t offset;
 };
 
-template <typename R, int PARTS, int MODE>
-__global__ void __launch_bounds__(256) k_external_product(KParams kp, Tables T, EpArgs a) {
+template <typename R, int PARTS, int MODE, int GROUPS, int L>
+__global__ void __launch_bounds__(64 * GROUPS, 1) k_external_product(KParams kp, Tables T, EpArgs a) {
+    constexpr int NB = L > PARTS ? L : PARTS;
+    using Ctx = StepCtx<R, PARTS, NB>;
+    using Plan = SmemPlan<R, NB>;
     extern __shared__ __align__(16) char smem[];
     cpx<R>* tables = reinterpret_cast<cpx<R>*>(smem);
     load_tables<R>(tables, T);
@@ -243,24 +311,24 @@ __global__ void __launch_bounds__(256) k_external_product(KParams kp, Tables T, 
 
     const int g = threadIdx.x >> 6;
     const int t = threadIdx.x & 63;
-    const int groups = blockDim.x >> 6;
-    const int c = blockIdx.x * groups + g;
+    const int c = blockIdx.x * GROUPS + g;
     if (c >= a.count) return;
 
-    char* gbase = smem + SmemPlan<R>::tables + (size_t)g * SmemPlan<R>::group;
-    StepCtx<R, PARTS> S;
-    S.tw = tables;
-    S.psi = tables + 512;
+    char* gbase = smem + Plan::tables + (size_t)g * Plan::group;
+    Ctx S;
+    S.tw = twiddles_at<R>(tables);
+    S.psi = tables + kTabPsi;
     S.acc = reinterpret_cast<int32_t*>(gbase);
-    S.s = scratch_at<R>(gbase + SmemPlan<R>::acc);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+        S.s[b] = scratch_at<R>(gbase + Plan::acc + (size_t)b * 2 * kScratchStride * sizeof(cpx<R>));
     S.t = t;
     S.bar_id = 1 + g;
-    S.l = kp.l;
     S.Bgbit = kp.Bgbit;
     S.split = kp.split;
     S.offset = kp.offset;
 
-    const size_t gsw_elems = (size_t)2 * kp.l * 2 * PARTS * kHalf;
+    const size_t gsw_elems = (size_t)2 * L * 2 * PARTS * kHalf;
     const cpx<R>* gsw_base = reinterpret_cast<const cpx<R>*>(a.gsw);
 
     if (MODE == kEpBlindRotate) {
@@ -281,10 +349,15 @@ __global__ void __launch_bounds__(256) k_external_product(KParams kp, Tables T, 
         group_sync(S.bar_id);
         const int32_t* bara = a.bara ? a.bara + (size_t)c * n : nullptr;
         const int32_t* xs = a.x ? a.x + (size_t)c * (n + 1) : nullptr;
+        // the rotation amount of step i + 1 is loaded during step i
+        int a_next = bara ? bara[0] : mod_switch_2n(xs[0]);
+#pragma unroll 1
         for (int i = 0; i < n; ++i) {
-            const int ai = bara ? bara[i] : mod_switch_2n(xs[i]);
+            const int ai = a_next;
+            if (i + 1 < n) a_next = bara ? bara[i + 1] : mod_switch_2n(xs[i + 1]);
             if (ai == 0) continue;  // tfhe_blindRotate_FFT.cpp:114
-            ep_step<R, PARTS, true>(S, gsw_base + (size_t)i * gsw_elems, ai);
+            const GlobalKeys<R, PARTS> keys{gsw_base + (size_t)i * gsw_elems};
+            ep_step<R, PARTS, true, L, L, PARTS, NB>(S, keys, ai);
         }
         if (a.acc_out) {
             int32_t* dst = a.acc_out + (size_t)c * 2 * kN;
@@ -303,14 +376,168 @@ __global__ void __launch_bounds__(256) k_external_product(KParams kp, Tables T, 
         group_sync(S.bar_id);
         const cpx<R>* gsw = reinterpret_cast<const cpx<R>*>(
             reinterpret_cast<const char*>(a.gsw) + a.gsw_stride * (size_t)c);
+        const GlobalKeys<R, PARTS> keys{gsw};
         if (MODE == kEpPlain) {
-            ep_step<R, PARTS, false>(S, gsw, 0);
+            ep_step<R, PARTS, false, L, L, PARTS, NB>(S, keys, 0);
         } else {
             const int ai = a.bara[c];
-            if (ai != 0) ep_step<R, PARTS, true>(S, gsw, ai);
+            if (ai != 0) ep_step<R, PARTS, true, L, L, PARTS, NB>(S, keys, ai);
         }
         int32_t* dst = a.acc_out + (size_t)c * 2 * kN;
         for (int i = t; i < 2 * kN; i += 64) dst[i] = S.acc[i];
+    }
+}
+
+// ----------------------------------------------------------------------
+// Blind rotation with the bootstrapping key streamed through shared memory.
+//
+// A CTA runs GROUPS ciphertexts (64 threads each) plus one producer warp.
+// Every ciphertext of the CTA walks the same key rows in the same order
+// (row r = step i * 2l + p), so the producer streams each 16 KB row once per
+// CTA with a bulk copy into a ring of S slots, and all groups read it from
+// shared memory: one key read per CTA instead of one per ciphertext, and no
+// L2 latency on the multiply-accumulate.  Slot hand-off uses two mbarriers
+// per slot: full (the copy's byte count landed) and empty (every consumer
+// thread has read the row).  A group that skips a step (a_i = 0) still waits
+// and releases its rows, so the ring stays in step.  Every wait is bounded;
+// a timeout sets *err (TFHE_GPU_TIMEOUT for the host) and the kernel runs to
+// its end without further waiting on the ring.
+// ----------------------------------------------------------------------
+template <typename R, int PARTS, int S>
+struct RingKeys {
+    static constexpr size_t kRow = (size_t)2 * PARTS * kHalf;
+    static constexpr bool kShared = true;
+    const cpx<R>* ring;
+    uint64_t* full;
+    uint64_t* empty;
+    uint32_t row0;
+    int32_t* err;
+    __device__ __forceinline__ void prefetch(int, int, int) const {}
+    __device__ __forceinline__ const cpx<R>* acquire(int p) const {
+        const uint32_t r = row0 + (uint32_t)p;
+        const uint32_t slot = r % S;
+        if (!mbar_wait_bounded(&full[slot], (r / S) & 1)) atomicExch(err, 3);
+        return ring + slot * kRow;
+    }
+    __device__ __forceinline__ void release(int p) const { mbar_arrive(&empty[(row0 + (uint32_t)p) % S]); }
+};
+
+template <typename R, int PARTS, int GROUPS, int L, int S>
+struct RingPlan {
+    static constexpr size_t kRowBytes = (size_t)2 * PARTS * kHalf * sizeof(cpx<R>);
+    static constexpr size_t tables = kTabSize * sizeof(cpx<R>);
+    static constexpr size_t ring_off = (tables + 127) & ~(size_t)127;
+    static constexpr size_t bar_off = ring_off + S * kRowBytes;
+    static constexpr size_t group_off = bar_off + 2 * S * sizeof(uint64_t);
+    static constexpr size_t acc = 2 * kN * sizeof(int32_t);
+    static constexpr size_t group = acc + 2 * kScratchStride * sizeof(cpx<R>);
+    static constexpr size_t total = group_off + GROUPS * group;
+};
+
+template <typename R, int PARTS, int GROUPS, int L, int S>
+__global__ void __launch_bounds__(64 * GROUPS + 32, 1)
+    k_blind_rotate_ring(KParams kp, Tables T, EpArgs a) {
+    using Plan = RingPlan<R, PARTS, GROUPS, L, S>;
+    constexpr int kpl = 2 * L;
+    extern __shared__ __align__(128) char smem[];
+    cpx<R>* tables = reinterpret_cast<cpx<R>*>(smem);
+    cpx<R>* ring = reinterpret_cast<cpx<R>*>(smem + Plan::ring_off);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + Plan::bar_off);
+    uint64_t* empty = full + S;
+    const int active = min(GROUPS, a.count - (int)blockIdx.x * GROUPS);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < S; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 64 * active);
+        }
+        fence_mbar_init();
+    }
+    load_tables<R>(tables, T);
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5;
+    const int n = kp.n;
+    if (warp == 2 * GROUPS) {
+        // producer warp: one lane streams all n * 2l key rows in order
+        if ((threadIdx.x & 31) == 0) {
+            const char* src = reinterpret_cast<const char*>(a.gsw);
+            const uint32_t total = (uint32_t)n * kpl;
+            uint32_t issued = 0;
+            for (uint32_t r = 0; r < total; ++r) {
+                const uint32_t slot = r % S;
+                if (r >= S && !mbar_wait_bounded(&empty[slot], ((r / S) - 1) & 1)) {
+                    atomicExch(a.err, 3);
+                    break;
+                }
+                mbar_arrive_expect_tx(&full[slot], (uint32_t)Plan::kRowBytes);
+                bulk_copy_g2s(reinterpret_cast<char*>(ring) + slot * Plan::kRowBytes,
+                              src + (size_t)r * Plan::kRowBytes, (uint32_t)Plan::kRowBytes,
+                              &full[slot]);
+                issued = r + 1;
+            }
+            // do not leave the CTA with copies still landing in its memory
+            for (uint32_t r = issued > S ? issued - S : 0; r < issued; ++r)
+                if (!mbar_wait_bounded(&full[r % S], (r / S) & 1)) atomicExch(a.err, 3);
+        }
+        return;
+    }
+
+    const int g = threadIdx.x >> 6;
+    const int t = threadIdx.x & 63;
+    const int c = blockIdx.x * GROUPS + g;
+    if (g >= active) return;
+
+    char* gbase = smem + Plan::group_off + (size_t)g * Plan::group;
+    StepCtx<R, PARTS, 1> St;
+    St.tw = twiddles_at<R>(tables);
+    St.psi = tables + kTabPsi;
+    St.acc = reinterpret_cast<int32_t*>(gbase);
+    St.s[0] = scratch_at<R>(gbase + Plan::acc);
+    St.t = t;
+    St.bar_id = 1 + g;
+    St.Bgbit = kp.Bgbit;
+    St.split = kp.split;
+    St.offset = kp.offset;
+
+    if (a.acc_in) {
+        const int32_t* src = a.acc_in + (size_t)c * 2 * kN;
+        for (int i = t; i < 2 * kN; i += 64) St.acc[i] = src[i];
+    } else {
+        const int32_t* xs = a.x + (size_t)c * (n + 1);
+        const int barb = mod_switch_2n(xs[n]);
+        for (int i = t; i < kN; i += 64) {
+            St.acc[i] = 0;
+            St.acc[kN + i] = (((i + barb) & (2 * kN - 1)) < kN) ? a.mu : -a.mu;
+        }
+    }
+    group_sync(St.bar_id);
+    const int32_t* bara = a.bara ? a.bara + (size_t)c * n : nullptr;
+    const int32_t* xs = a.x ? a.x + (size_t)c * (n + 1) : nullptr;
+    RingKeys<R, PARTS, S> keys{ring, full, empty, 0, a.err};
+    int a_next = bara ? bara[0] : mod_switch_2n(xs[0]);
+#pragma unroll 1
+    for (int i = 0; i < n; ++i) {
+        const int ai = a_next;
+        if (i + 1 < n) a_next = bara ? bara[i + 1] : mod_switch_2n(xs[i + 1]);
+        keys.row0 = (uint32_t)i * kpl;
+        if (ai == 0) {  // tfhe_blindRotate_FFT.cpp:114 -- rows still pass through
+            for (int p = 0; p < kpl; ++p) {
+                keys.acquire(p);
+                keys.release(p);
+            }
+            continue;
+        }
+        ep_step<R, PARTS, true, L, 1, 1, 1>(St, keys, ai);
+    }
+    if (a.acc_out) {
+        int32_t* dst = a.acc_out + (size_t)c * 2 * kN;
+        for (int i = t; i < 2 * kN; i += 64) dst[i] = St.acc[i];
+    }
+    if (a.lwe_out) {
+        int32_t* dst = a.lwe_out + (size_t)c * (kN + 1);
+        for (int i = t; i < kN; i += 64)
+            dst[i] = i == 0 ? St.acc[0] : (int32_t)(0u - (uint32_t)St.acc[kN - i]);
+        if (t == 0) dst[kN] = St.acc[kN];
     }
 }
 
@@ -319,7 +546,7 @@ __global__ void __launch_bounds__(256) k_external_product(KParams kp, Tables T, 
 // ----------------------------------------------------------------------
 __device__ __forceinline__ void twisted_forward64(const double* coef, cpx<double> (&v)[8],
                                                   const FftScratch<double>& s,
-                                                  const cpx<double>* tw,
+                                                  const FftTwiddles<double>& tw,
                                                   const cpx<double>* psi, int t, int bar) {
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
@@ -330,7 +557,8 @@ __device__ __forceinline__ void twisted_forward64(const double* coef, cpx<double
 }
 
 // Per polynomial smem: 1024 doubles of coefficients + scratch.
-constexpr size_t kConvGroupBytes = kN * sizeof(double) + 4 * kScratchStride * sizeof(double);
+constexpr size_t kConvGroupBytes = kN * sizeof(double) + 2 * kScratchStride * sizeof(cpx<double>);
+constexpr size_t kConvTableBytes = kTabSize * sizeof(cpx<double>);
 
 template <int FORM>
 __global__ void __launch_bounds__(256) k_tgsw_to_fft(Tables T, const int32_t* __restrict__ in,
@@ -342,7 +570,7 @@ __global__ void __launch_bounds__(256) k_tgsw_to_fft(Tables T, const int32_t* __
     const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
     const int poly = blockIdx.x * (blockDim.x >> 6) + g;
     if (poly >= npoly) return;
-    char* gbase = smem + 1024 * sizeof(cpx<double>) + (size_t)g * kConvGroupBytes;
+    char* gbase = smem + kConvTableBytes + (size_t)g * kConvGroupBytes;
     double* coef = reinterpret_cast<double*>(gbase);
     FftScratch<double> s = scratch_at<double>(gbase + kN * sizeof(double));
     const int32_t* src = in + (size_t)poly * kN;
@@ -352,7 +580,7 @@ __global__ void __launch_bounds__(256) k_tgsw_to_fft(Tables T, const int32_t* __
         for (int i = t; i < kN; i += 64) coef[i] = (double)src[i];
         group_sync(bar);
         cpx<double> v[8];
-        twisted_forward64(coef, v, s, tables, tables + 512, t, bar);
+        twisted_forward64(coef, v, s, twiddles_at<double>(tables), tables + kTabPsi, t, bar);
         cpx<double>* dst = reinterpret_cast<cpx<double>*>(out) + (size_t)poly * kHalf;
 #pragma unroll
         for (int q = 0; q < 8; ++q) dst[key_index<double>(t, q)] = v[q];
@@ -369,7 +597,7 @@ __global__ void __launch_bounds__(256) k_tgsw_to_fft(Tables T, const int32_t* __
             }
             group_sync(bar);
             cpx<double> v[8];
-            twisted_forward64(coef, v, s, tables, tables + 512, t, bar);
+            twisted_forward64(coef, v, s, twiddles_at<double>(tables), tables + kTabPsi, t, bar);
 #pragma unroll
             for (int q = 0; q < 8; ++q)
                 dst[part * kHalf + key_index<float>(t, q)] = {(float)v[q].x, (float)v[q].y};
@@ -388,17 +616,17 @@ __global__ void __launch_bounds__(256) k_fft64_to_tgsw(Tables T, const void* in,
     const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
     const int poly = blockIdx.x * (blockDim.x >> 6) + g;
     if (poly >= npoly) return;
-    char* gbase = smem + 1024 * sizeof(cpx<double>) + (size_t)g * kConvGroupBytes;
+    char* gbase = smem + kConvTableBytes + (size_t)g * kConvGroupBytes;
     FftScratch<double> s = scratch_at<double>(gbase + kN * sizeof(double));
     const cpx<double>* src = reinterpret_cast<const cpx<double>*>(in) + (size_t)poly * kHalf;
     cpx<double> v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) v[q] = src[key_index<double>(t, q)];
-    fft512_inverse(v, s, tables, t, 1 + g);
+    fft512_inverse(v, s, twiddles_at<double>(tables), t, 1 + g);
     int32_t* dst = out + (size_t)poly * kN;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        const cpx<double> z = cmulc(v[q], tables[512 + t + 64 * q]);
+        const cpx<double> z = cmulc(v[q], tables[kTabPsi + t + 64 * q]);
         dst[t + 64 * q] = (int32_t)(uint32_t)(uint64_t)llrint(z.x / 512.0);
         dst[t + 64 * q + kHalf] = (int32_t)(uint32_t)(uint64_t)llrint(z.y / 512.0);
     }
@@ -431,14 +659,14 @@ __global__ void __launch_bounds__(256) k_poly_to_lagrange(Tables T, const int32_
     const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
     const int poly = blockIdx.x * (blockDim.x >> 6) + g;
     if (poly >= npoly) return;
-    char* gbase = smem + 1024 * sizeof(cpx<double>) + (size_t)g * kConvGroupBytes;
+    char* gbase = smem + kConvTableBytes + (size_t)g * kConvGroupBytes;
     double* coef = reinterpret_cast<double*>(gbase);
     FftScratch<double> s = scratch_at<double>(gbase + kN * sizeof(double));
     const int32_t* src = in + (size_t)poly * kN;
     for (int i = t; i < kN; i += 64) coef[i] = (double)src[i];
     group_sync(1 + g);
     cpx<double> v[8];
-    twisted_forward64(coef, v, s, tables, tables + 512, t, 1 + g);
+    twisted_forward64(coef, v, s, twiddles_at<double>(tables), tables + kTabPsi, t, 1 + g);
     double* dst = out + (size_t)poly * kN;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -461,7 +689,7 @@ __global__ void __launch_bounds__(256) k_lagrange_to_torus(Tables T, const doubl
     const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
     const int poly = blockIdx.x * (blockDim.x >> 6) + g;
     if (poly >= npoly) return;
-    char* gbase = smem + 1024 * sizeof(cpx<double>) + (size_t)g * kConvGroupBytes;
+    char* gbase = smem + kConvTableBytes + (size_t)g * kConvGroupBytes;
     FftScratch<double> s = scratch_at<double>(gbase + kN * sizeof(double));
     const double* src = in + (size_t)poly * kN;
     cpx<double> v[8];
@@ -473,12 +701,12 @@ __global__ void __launch_bounds__(256) k_lagrange_to_torus(Tables T, const doubl
         const double re = src[2 * ref], im = src[2 * ref + 1];
         v[q] = {re, cj ? -im : im};
     }
-    fft512_inverse(v, s, tables, t, 1 + g);
+    fft512_inverse(v, s, twiddles_at<double>(tables), t, 1 + g);
     const double sc = 4294967296.0 / 512.0;
     int32_t* dst = out + (size_t)poly * kN;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        const cpx<double> z = cmulc(v[q], tables[512 + t + 64 * q]);
+        const cpx<double> z = cmulc(v[q], tables[kTabPsi + t + 64 * q]);
         dst[t + 64 * q] = (int32_t)(uint32_t)(uint64_t)__double2ll_rz(z.x * sc);
         dst[t + 64 * q + kHalf] = (int32_t)(uint32_t)(uint64_t)__double2ll_rz(z.y * sc);
     }
@@ -608,23 +836,65 @@ uint32_t decomp_offset(int l, int Bgbit) {
     return o * (uint32_t)(1 << (Bgbit - 1));
 }
 
-template <typename R, int PARTS, int MODE>
-cudaError_t launch_ep_t(const DevParams& P, const Tables& T, const EpArgs& a, int groups,
-                        cudaStream_t st) {
+template <typename R, int PARTS, int MODE, int GROUPS, int L>
+cudaError_t launch_ep_t(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
     if (a.count <= 0) return cudaSuccess;
     KParams kp;
     kp.n = P.n;
-    kp.l = P.l;
     kp.Bgbit = P.Bgbit;
     kp.split = P.split_bits;
     kp.offset = decomp_offset(P.l, P.Bgbit);
-    const size_t smem = SmemPlan<R>::total(groups);
-    auto kern = k_external_product<R, PARTS, MODE>;
+    const size_t smem = SmemPlan<R, (L > PARTS ? L : PARTS)>::total(GROUPS);
+    auto kern = k_external_product<R, PARTS, MODE, GROUPS, L>;
     cudaError_t e = set_smem(kern, smem);
     if (e != cudaSuccess) return e;
-    const int grid = (a.count + groups - 1) / groups;
-    kern<<<grid, 64 * groups, smem, st>>>(kp, T, a);
+    const int grid = (a.count + GROUPS - 1) / GROUPS;
+    kern<<<grid, 64 * GROUPS, smem, st>>>(kp, T, a);
     return cudaGetLastError();
+}
+
+template <typename R, int PARTS, int GROUPS, int L>
+cudaError_t launch_ring_t(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
+    constexpr int S = 4;
+    if (a.count <= 0) return cudaSuccess;
+    KParams kp;
+    kp.n = P.n;
+    kp.Bgbit = P.Bgbit;
+    kp.split = P.split_bits;
+    kp.offset = decomp_offset(P.l, P.Bgbit);
+    using Plan = RingPlan<R, PARTS, GROUPS, L, S>;
+    auto kern = k_blind_rotate_ring<R, PARTS, GROUPS, L, S>;
+    cudaError_t e = set_smem(kern, Plan::total);
+    if (e != cudaSuccess) return e;
+    const int grid = (a.count + GROUPS - 1) / GROUPS;
+    kern<<<grid, 64 * GROUPS + 32, Plan::total, st>>>(kp, T, a);
+    return cudaGetLastError();
+}
+
+// FP64: ~250 registers per thread and 2 x L exchange buffers of 9 KB per
+// group, so 3 groups (192 threads) per CTA.  split-FP32: GROUPS groups.
+template <int L>
+cudaError_t launch_ep_l(const DevParams& P, Form f, EpMode mode, const Tables& T, const EpArgs& a,
+                        int groups, cudaStream_t st) {
+    if (f == kFormFp64) {
+        switch (mode) {
+        case kEpPlain: return launch_ep_t<double, 1, kEpPlain, 3, L>(P, T, a, st);
+        case kEpMuxRotate: return launch_ep_t<double, 1, kEpMuxRotate, 3, L>(P, T, a, st);
+        default:
+            if (groups == 3) return launch_ep_t<double, 1, kEpBlindRotate, 3, L>(P, T, a, st);
+            return launch_ring_t<double, 1, 4, L>(P, T, a, st);
+        }
+    }
+    switch (mode) {
+    case kEpPlain: return launch_ep_t<float, 2, kEpPlain, 4, L>(P, T, a, st);
+    case kEpMuxRotate: return launch_ep_t<float, 2, kEpMuxRotate, 4, L>(P, T, a, st);
+    default:
+        // groups 4 / 6: the L2-direct kernel; 5 / 8: the shared-ring kernel
+        if (groups == 4) return launch_ep_t<float, 2, kEpBlindRotate, 4, L>(P, T, a, st);
+        if (groups == 6) return launch_ep_t<float, 2, kEpBlindRotate, 6, L>(P, T, a, st);
+        if (groups == 8) return launch_ring_t<float, 2, 8, L>(P, T, a, st);
+        return launch_ring_t<float, 2, 5, L>(P, T, a, st);
+    }
 }
 
 }  // namespace
@@ -655,9 +925,18 @@ static void sincos_2pi_frac(long k, long M, double* c, double* s) {
 }
 
 void make_twiddles_host(double* h) {
-    for (int k = 0; k < 512; ++k) sincos_2pi_frac(k, 512, &h[2 * k], &h[2 * k + 1]);
-    for (int x = 0; x < 512; ++x) sincos_2pi_frac(x, 2048, &h[1024 + 2 * x], &h[1024 + 2 * x + 1]);
+    // layout of Tables: [q][t] W^(tq) | [q][j] W^(8jq) | psi^x, W = e^{2 pi i/512}
+    for (int q = 0; q < 8; ++q)
+        for (int t = 0; t < 64; ++t)
+            sincos_2pi_frac(t * q, 512, &h[2 * (kTabA + q * 64 + t)], &h[2 * (kTabA + q * 64 + t) + 1]);
+    for (int q = 0; q < 8; ++q)
+        for (int j = 0; j < 8; ++j)
+            sincos_2pi_frac(8 * j * q, 512, &h[2 * (kTabB + q * 8 + j)], &h[2 * (kTabB + q * 8 + j) + 1]);
+    for (int x = 0; x < 512; ++x)
+        sincos_2pi_frac(x, 2048, &h[2 * (kTabPsi + x)], &h[2 * (kTabPsi + x) + 1]);
 }
+
+int twiddle_table_entries() { return kTabSize; }
 
 size_t tgsw_fft_bytes(const DevParams& P, Form f) {
     const size_t rows = (size_t)(P.k + 1) * P.l;
@@ -670,7 +949,7 @@ cudaError_t launch_tgsw_to_fft(const DevParams& P, Form f, const Tables& T, cons
     const int npoly = count * (P.k + 1) * P.l * (P.k + 1);
     if (npoly <= 0) return cudaSuccess;
     const int groups = 4;
-    const size_t smem = 1024 * sizeof(cpx<double>) + groups * kConvGroupBytes;
+    const size_t smem = kConvTableBytes + groups * kConvGroupBytes;
     const int grid = (npoly + groups - 1) / groups;
     cudaError_t e;
     if (f == kFormFp64) {
@@ -691,7 +970,7 @@ cudaError_t launch_tgsw_from_fft64(const DevParams& P, const Tables& T, const vo
     const int npoly = count * (P.k + 1) * P.l * (P.k + 1);
     if (npoly <= 0) return cudaSuccess;
     const int groups = 4;
-    const size_t smem = 1024 * sizeof(cpx<double>) + groups * kConvGroupBytes;
+    const size_t smem = kConvTableBytes + groups * kConvGroupBytes;
     cudaError_t e = set_smem(k_fft64_to_tgsw, smem);
     if (e != cudaSuccess) return e;
     k_fft64_to_tgsw<<<(npoly + groups - 1) / groups, 64 * groups, smem, st>>>(T, in, tgsw, npoly);
@@ -718,19 +997,10 @@ cudaError_t launch_engine64_to_lagrange_ref(const void* eng, double* ref, int np
 
 cudaError_t launch_external_product(const DevParams& P, Form f, EpMode mode, const Tables& T,
                                     const EpArgs& a, int groups, cudaStream_t st) {
-    if (groups < 1) groups = 1;
-    if (groups > 4) groups = 4;
-    if (f == kFormFp64) {
-        switch (mode) {
-        case kEpPlain: return launch_ep_t<double, 1, kEpPlain>(P, T, a, groups, st);
-        case kEpMuxRotate: return launch_ep_t<double, 1, kEpMuxRotate>(P, T, a, groups, st);
-        default: return launch_ep_t<double, 1, kEpBlindRotate>(P, T, a, groups, st);
-        }
-    }
-    switch (mode) {
-    case kEpPlain: return launch_ep_t<float, 2, kEpPlain>(P, T, a, groups, st);
-    case kEpMuxRotate: return launch_ep_t<float, 2, kEpMuxRotate>(P, T, a, groups, st);
-    default: return launch_ep_t<float, 2, kEpBlindRotate>(P, T, a, groups, st);
+    switch (P.l) {
+    case 2: return launch_ep_l<2>(P, f, mode, T, a, groups, st);
+    case 3: return launch_ep_l<3>(P, f, mode, T, a, groups, st);
+    default: return cudaErrorInvalidValue;  // decomposition lengths 2 and 3 are built
     }
 }
 
@@ -776,7 +1046,7 @@ cudaError_t launch_poly_to_lagrange(const DevParams& P, const Tables& T, const i
     (void)P;
     if (count <= 0) return cudaSuccess;
     const int groups = 4;
-    const size_t smem = 1024 * sizeof(cpx<double>) + groups * kConvGroupBytes;
+    const size_t smem = kConvTableBytes + groups * kConvGroupBytes;
     cudaError_t e = set_smem(k_poly_to_lagrange, smem);
     if (e != cudaSuccess) return e;
     k_poly_to_lagrange<<<(count + groups - 1) / groups, 64 * groups, smem, st>>>(T, in, out, count,
@@ -789,7 +1059,7 @@ cudaError_t launch_lagrange_to_torus(const DevParams& P, const Tables& T, const 
     (void)P;
     if (count <= 0) return cudaSuccess;
     const int groups = 4;
-    const size_t smem = 1024 * sizeof(cpx<double>) + groups * kConvGroupBytes;
+    const size_t smem = kConvTableBytes + groups * kConvGroupBytes;
     cudaError_t e = set_smem(k_lagrange_to_torus, smem);
     if (e != cudaSuccess) return e;
     k_lagrange_to_torus<<<(count + groups - 1) / groups, 64 * groups, smem, st>>>(T, in, out,

@@ -60,12 +60,12 @@ bool params_supported(const tfhe_params* P, std::string* why) {
     if (P->N != 1024) { *why = "only N = 1024 is built"; return false; }
     if (P->k != 1) { *why = "only k = 1 is built"; return false; }
     if (P->n < 1 || P->n > 4096) { *why = "n out of range"; return false; }
-    if (P->l < 1 || P->l > 8 || P->Bgbit < 1 || P->l * P->Bgbit > 32) {
-        *why = "bad decomposition (l, Bgbit)";
+    if (P->l < 2 || P->l > 3 || P->Bgbit < 1 || P->l * P->Bgbit > 32) {
+        *why = "bad decomposition (l in {2, 3} is built, l * Bgbit <= 32)";
         return false;
     }
-    if (P->ks_basebit < 1 || P->ks_basebit > 2 || P->ks_t < 1 || P->ks_t * P->ks_basebit > 31) {
-        *why = "bad key-switch decomposition (t, basebit <= 2)";
+    if (P->ks_basebit != 2 || P->ks_t < 4 || P->ks_t > 12 || P->ks_t % 4) {
+        *why = "key switch built for basebit = 2, t in {4, 8, 12}";
         return false;
     }
     if (P->split_bits < 0 || P->split_bits > 31) { *why = "split_bits out of range"; return false; }
@@ -89,6 +89,16 @@ tfhe_gpu_status ensure_scratch(tfhe_gpu_ctx* ctx, int slot, size_t bytes, void**
 }
 
 bool form_ok(int32_t form) { return form == TFHE_GPU_FP64 || form == TFHE_GPU_SPLIT_FP32; }
+
+// After a synchronisation: a kernel whose bounded wait ran out leaves 3 in
+// the device status word.  Report it once and clear it.
+tfhe_gpu_status check_device_status(tfhe_gpu_ctx* ctx) {
+    int32_t v = 0;
+    CK(ctx, cudaMemcpy(&v, ctx->d_err, sizeof(v), cudaMemcpyDeviceToHost));
+    if (v == 0) return TFHE_GPU_OK;
+    CK(ctx, cudaMemset(ctx->d_err, 0, sizeof(int32_t)));
+    return fail(ctx, TFHE_GPU_TIMEOUT, "a bounded wait in a kernel gave up (key-row ring stalled)");
+}
 
 tfhe_gpu_status need_bk(tfhe_gpu_ctx* ctx, int32_t form) {
     if (!form_ok(form)) return fail(ctx, TFHE_GPU_BAD_PARAM, "unknown form");
@@ -118,6 +128,7 @@ tfhe_gpu_status set_device(tfhe_gpu_ctx* ctx) {
 tfhe_gpu_status run_bootstrap_woks(tfhe_gpu_ctx* ctx, const int32_t* x, int32_t mu, int32_t* u,
                                    int32_t count, int32_t form, cudaStream_t st) {
     EpArgs a{};
+    a.err = ctx->d_err;
     a.x = x;
     a.mu = mu;
     a.lwe_out = u;
@@ -198,11 +209,12 @@ tfhe_gpu_status tfhe_gpu_create(const tfhe_params* params, int32_t device, tfhe_
     if (cudaSetDevice(device) != cudaSuccess) return bail(TFHE_GPU_DEVICE_ERROR);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
         return bail(TFHE_GPU_DEVICE_ERROR);
-    std::vector<double> h64(2048);
+    const int nt = 2 * twiddle_table_entries();
+    std::vector<double> h64(nt);
     make_twiddles_host(h64.data());
-    std::vector<float> h32(2048);
-    for (int i = 0; i < 2048; ++i) h32[i] = (float)h64[i];
-    const size_t b64 = 2048 * sizeof(double), b32 = 2048 * sizeof(float);
+    std::vector<float> h32(nt);
+    for (int i = 0; i < nt; ++i) h32[i] = (float)h64[i];
+    const size_t b64 = nt * sizeof(double), b32 = nt * sizeof(float);
     if (cudaMalloc(&ctx->d_tables, b64 + b32) != cudaSuccess) return bail(TFHE_GPU_OOM);
     if (cudaMemcpy(ctx->d_tables, h64.data(), b64, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy((char*)ctx->d_tables + b64, h32.data(), b32, cudaMemcpyHostToDevice) !=
@@ -211,6 +223,8 @@ tfhe_gpu_status tfhe_gpu_create(const tfhe_params* params, int32_t device, tfhe_
     ctx->tables.tw64 = ctx->d_tables;
     ctx->tables.tw32 = (char*)ctx->d_tables + b64;
     ctx->key_bytes = b64 + b32;
+    if (cudaMalloc(&ctx->d_err, sizeof(int32_t)) != cudaSuccess) return bail(TFHE_GPU_OOM);
+    if (cudaMemset(ctx->d_err, 0, sizeof(int32_t)) != cudaSuccess) return bail(TFHE_GPU_DEVICE_ERROR);
     *out = ctx;
     return TFHE_GPU_OK;
 }
@@ -225,6 +239,7 @@ void tfhe_gpu_destroy(tfhe_gpu_ctx* ctx) {
     for (int s = 0; s < 4; ++s)
         if (ctx->d_scratch[s]) cudaFree(ctx->d_scratch[s]);
     if (ctx->d_tables) cudaFree(ctx->d_tables);
+    if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -244,7 +259,7 @@ void* tfhe_gpu_stream(const tfhe_gpu_ctx* ctx) { return ctx ? (void*)ctx->stream
 tfhe_gpu_status tfhe_gpu_synchronize(tfhe_gpu_ctx* ctx) {
     CHECK_CTX(ctx);
     CK(ctx, cudaStreamSynchronize(ctx->stream));
-    return TFHE_GPU_OK;
+    return check_device_status(ctx);
 }
 
 size_t tfhe_gpu_tgsw_fft_bytes(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form) {
@@ -257,6 +272,21 @@ size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx) {
     size_t b = ctx->key_bytes;
     for (int s = 0; s < 4; ++s) b += ctx->scratch_bytes[s];
     return b;
+}
+
+tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,
+                                            int32_t groups) {
+    if (!ctx || !form_ok(form)) return TFHE_GPU_BAD_PARAM;
+    const bool ok = form == TFHE_GPU_FP64 ? (groups == 3 || groups == 4)
+                                          : (groups == 4 || groups == 5 || groups == 6 || groups == 8);
+    if (!ok) return fail(ctx, TFHE_GPU_BAD_PARAM, "unsupported groups per CTA for this form");
+    ctx->groups_per_cta[form] = groups;
+    return TFHE_GPU_OK;
+}
+
+int32_t tfhe_gpu_get_groups_per_cta(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form) {
+    if (!ctx || !form_ok(form)) return 0;
+    return ctx->groups_per_cta[form];
 }
 
 // ---- keys -------------------------------------------------------------
@@ -406,6 +436,7 @@ tfhe_gpu_status tfhe_gpu_tGswFFTExternMulToTLwe(tfhe_gpu_ctx* ctx, int32_t* accu
     if (!form_ok(form) || count < 0 || (count && (!accum || !gsw)))
         return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
     EpArgs a{};
+    a.err = ctx->d_err;
     a.acc_in = accum;
     a.acc_out = accum;
     a.gsw = gsw;
@@ -424,6 +455,7 @@ tfhe_gpu_status tfhe_gpu_tfhe_MuxRotate_FFT(tfhe_gpu_ctx* ctx, int32_t* result,
     if (!form_ok(form) || count < 0 || (count && (!result || !accum || !gsw || !barai)))
         return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
     EpArgs a{};
+    a.err = ctx->d_err;
     a.acc_in = accum;
     a.acc_out = result;
     a.bara = barai;
@@ -442,6 +474,7 @@ tfhe_gpu_status tfhe_gpu_tfhe_blindRotate_FFT(tfhe_gpu_ctx* ctx, int32_t* accum,
     RET(need_bk(ctx, form));
     if (count < 0 || (count && (!accum || !bara))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
     EpArgs a{};
+    a.err = ctx->d_err;
     a.acc_in = accum;
     a.acc_out = accum;
     a.bara = bara;
@@ -566,7 +599,7 @@ tfhe_gpu_status tfhe_gpu_bootsGates_host(tfhe_gpu_ctx* ctx, const int32_t* gates
     RET(run_gates(ctx, (const int32_t*)d_g, uniform_gate, d_out, d_ca, d_cb, count, form, st));
     CK(ctx, cudaMemcpyAsync(out, d_out, lwe_bytes, cudaMemcpyDeviceToHost, st));
     CK(ctx, cudaStreamSynchronize(st));
-    return TFHE_GPU_OK;
+    return check_device_status(ctx);
 }
 
 }  // extern "C"

@@ -18,7 +18,7 @@ struct tfhe_gpu_ctx {
     DevParams dp;
     int device = 0;
     cudaStream_t stream = nullptr;
-    void* d_tables = nullptr;  // 1024 double2 then 1024 float2
+    void* d_tables = nullptr;  // transform tables: FP64 copy then FP32 copy
     Tables tables{};
     void* d_bk[kNumForms] = {nullptr, nullptr};
     int32_t* d_ks = nullptr;
@@ -26,7 +26,8 @@ struct tfhe_gpu_ctx {
     // scratch slots, grown on demand
     void* d_scratch[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t scratch_bytes[4] = {0, 0, 0, 0};
-    int groups_per_cta[kNumForms] = {4, 4};
+    int groups_per_cta[kNumForms] = {3, 5};  // ciphertexts per CTA (64 threads each)
+    int32_t* d_err = nullptr;  // device status word written by bounded waits (3 = timeout)
     std::string last_error;
     size_t key_bytes = 0;
 };

@@ -23,13 +23,16 @@ struct DevParams {
 // Bytes of one TGSW sample (kpl rows x 2 polys) in the engine FFT layout.
 size_t tgsw_fft_bytes(const DevParams& P, Form f);
 
-// Twiddle tables: [0,512) = e^{+2 pi i k/512}, [512,1024) = e^{i pi x/1024}.
-// `host64` holds 2048 doubles (re, im interleaved).
+// Transform tables, twiddle_table_entries() complex values: the radix-8
+// passes' twiddles W^(tq) and W^(8jq) (W = e^{2 pi i/512}) in the order the
+// threads read them, then psi^x = e^{i pi x/1024}.  `host64` receives
+// 2 * twiddle_table_entries() doubles (re, im interleaved).
+int twiddle_table_entries();
 void make_twiddles_host(double* host64);
 
 struct Tables {
-    const void* tw64;  // 1024 double2
-    const void* tw32;  // 1024 float2
+    const void* tw64;  // twiddle_table_entries() double2
+    const void* tw32;  // twiddle_table_entries() float2
 };
 
 // TGSW (time domain, count x kpl x 2 x N int32) -> engine FFT layout.
@@ -68,6 +71,7 @@ struct EpArgs {
     const void* gsw;
     size_t gsw_stride;
     int count;
+    int32_t* err;  // device status word: set to 3 (timeout) by a bounded wait
 };
 
 cudaError_t launch_external_product(const DevParams& P, Form f, EpMode mode,

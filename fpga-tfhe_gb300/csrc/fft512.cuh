@@ -20,8 +20,9 @@
 //   product works in that order; the key is stored in it, so no reordering.
 //   inverse (decimation in time) runs the passes backwards, input from
 //   registers (positions 8t + q) to natural order (positions t + 64q).
-// Shared scratch: two ping-pong buffers, split re/im, padded p + p/8 so the
-// strided exchanges are (almost) free of bank conflicts.
+// Shared scratch: two ping-pong buffers of interleaved complex values, padded
+// p + p/8 so the strided exchanges are (almost) free of bank conflicts; the
+// twiddles are stored per pass in the order the threads read them.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -29,7 +30,7 @@
 namespace tfhe_gb300 {
 
 template <typename R>
-struct cpx {
+struct __align__(2 * sizeof(R)) cpx {
     R x, y;
 };
 
@@ -97,52 +98,46 @@ __device__ __forceinline__ void group_sync(int bar_id) {
     asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(kFftThreads) : "memory");
 }
 
+// Two ping-pong exchange buffers of kScratchStride interleaved complex values.
 template <typename R>
 struct FftScratch {
-    R* re0;
-    R* im0;
-    R* re1;
-    R* im1;
+    cpx<R>* b0;
+    cpx<R>* b1;
 };
 
+// Twiddles laid out so that a warp reads consecutive (or identical) words:
+//   a[q * 64 + t] = W^(t q)      pass A / A'   (W = e^{+2 pi i / 512})
+//   b[q * 8 + j]  = W^(8 j q)    pass B / B'
 template <typename R>
-__device__ __forceinline__ void sst(R* re, R* im, int p, cpx<R> v) {
-    const int q = spad(p);
-    re[q] = v.x;
-    im[q] = v.y;
-}
-template <typename R>
-__device__ __forceinline__ cpx<R> sld(const R* re, const R* im, int p) {
-    const int q = spad(p);
-    return {re[q], im[q]};
-}
+struct FftTwiddles {
+    const cpx<R>* a;
+    const cpx<R>* b;
+};
 
 // Forward transform.  In: v[r] = z[t + 64r].  Out: v[q] = position 8t + q.
-// tw[k] = e^{+2 pi i k / 512}.
 template <typename R>
 __device__ __forceinline__ void fft512_forward(cpx<R> (&v)[8], const FftScratch<R>& s,
-                                               const cpx<R>* __restrict__ tw, int t,
-                                               int bar_id) {
+                                               const FftTwiddles<R>& tw, int t, int bar_id) {
     // pass A
     dft8<1>(v);
 #pragma unroll
-    for (int q = 1; q < 8; ++q) v[q] = cmul(v[q], tw[(t * q) & 511]);
+    for (int q = 1; q < 8; ++q) v[q] = cmul(v[q], tw.a[q * 64 + t]);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) sst(s.re0, s.im0, t + 64 * q, v[q]);
+    for (int q = 0; q < 8; ++q) s.b0[spad(t + 64 * q)] = v[q];
     group_sync(bar_id);
     // pass B
     const int b = t >> 3, j = t & 7;
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = sld(s.re0, s.im0, 64 * b + j + 8 * r);
+    for (int r = 0; r < 8; ++r) v[r] = s.b0[spad(64 * b + j + 8 * r)];
     dft8<1>(v);
 #pragma unroll
-    for (int q = 1; q < 8; ++q) v[q] = cmul(v[q], tw[(8 * j * q) & 511]);
+    for (int q = 1; q < 8; ++q) v[q] = cmul(v[q], tw.b[q * 8 + j]);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) sst(s.re1, s.im1, 64 * b + j + 8 * q, v[q]);
+    for (int q = 0; q < 8; ++q) s.b1[spad(64 * b + j + 8 * q)] = v[q];
     group_sync(bar_id);
     // pass C
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = sld(s.re1, s.im1, 8 * t + r);
+    for (int r = 0; r < 8; ++r) v[r] = s.b1[spad(8 * t + r)];
     dft8<1>(v);
 }
 
@@ -150,31 +145,100 @@ __device__ __forceinline__ void fft512_forward(cpx<R> (&v)[8], const FftScratch<
 // 8t + q.  Out: v[q] = z[t + 64q].
 template <typename R>
 __device__ __forceinline__ void fft512_inverse(cpx<R> (&v)[8], const FftScratch<R>& s,
-                                               const cpx<R>* __restrict__ tw, int t,
-                                               int bar_id) {
+                                               const FftTwiddles<R>& tw, int t, int bar_id) {
     // pass C'
     dft8<-1>(v);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) sst(s.re0, s.im0, 8 * t + q, v[q]);
+    for (int q = 0; q < 8; ++q) s.b0[spad(8 * t + q)] = v[q];
     group_sync(bar_id);
     // pass B'
     const int b = t >> 3, j = t & 7;
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-        v[r] = sld(s.re0, s.im0, 64 * b + j + 8 * r);
-        if (r) v[r] = cmulc(v[r], tw[(8 * j * r) & 511]);
+        v[r] = s.b0[spad(64 * b + j + 8 * r)];
+        if (r) v[r] = cmulc(v[r], tw.b[r * 8 + j]);
     }
     dft8<-1>(v);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) sst(s.re1, s.im1, 64 * b + j + 8 * q, v[q]);
+    for (int q = 0; q < 8; ++q) s.b1[spad(64 * b + j + 8 * q)] = v[q];
     group_sync(bar_id);
     // pass A'
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-        v[r] = sld(s.re1, s.im1, t + 64 * r);
-        if (r) v[r] = cmulc(v[r], tw[(t * r) & 511]);
+        v[r] = s.b1[spad(t + 64 * r)];
+        if (r) v[r] = cmulc(v[r], tw.a[r * 64 + t]);
     }
     dft8<-1>(v);
+}
+
+// NB independent transforms at once (each with its own ping-pong pair of
+// buffers s[b]): the same three passes, but every pass works on NB point
+// sets before the group barrier, so each barrier phase carries NB times the
+// arithmetic and the registers hold NB independent dependency chains.
+template <int NB, typename R>
+__device__ __forceinline__ void fft512_forward_multi(cpx<R> (&v)[NB][8], const FftScratch<R> (&s)[NB],
+                                                     const FftTwiddles<R>& tw, int t, int bar_id) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        dft8<1>(v[b]);
+#pragma unroll
+        for (int q = 1; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.a[q * 64 + t]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s[b].b0[spad(t + 64 * q)] = v[b][q];
+    }
+    group_sync(bar_id);
+    const int hb = t >> 3, j = t & 7;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b0[spad(64 * hb + j + 8 * r)];
+        dft8<1>(v[b]);
+#pragma unroll
+        for (int q = 1; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.b[q * 8 + j]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s[b].b1[spad(64 * hb + j + 8 * q)] = v[b][q];
+    }
+    group_sync(bar_id);
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b1[spad(8 * t + r)];
+        dft8<1>(v[b]);
+    }
+}
+
+template <int NB, typename R>
+__device__ __forceinline__ void fft512_inverse_multi(cpx<R> (&v)[NB][8], const FftScratch<R> (&s)[NB],
+                                                     const FftTwiddles<R>& tw, int t, int bar_id) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        dft8<-1>(v[b]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s[b].b0[spad(8 * t + q)] = v[b][q];
+    }
+    group_sync(bar_id);
+    const int hb = t >> 3, j = t & 7;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            v[b][r] = s[b].b0[spad(64 * hb + j + 8 * r)];
+            if (r) v[b][r] = cmulc(v[b][r], tw.b[r * 8 + j]);
+        }
+        dft8<-1>(v[b]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s[b].b1[spad(64 * hb + j + 8 * q)] = v[b][q];
+    }
+    group_sync(bar_id);
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            v[b][r] = s[b].b1[spad(t + 64 * r)];
+            if (r) v[b][r] = cmulc(v[b][r], tw.a[r * 64 + t]);
+        }
+        dft8<-1>(v[b]);
+    }
 }
 
 // Frequency held at (thread t, register q) after the forward transform.

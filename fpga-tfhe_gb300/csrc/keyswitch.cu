@@ -9,72 +9,92 @@
 //
 // GB300 layout and schedule: the table is [kN][t][base][row_stride] int32
 // with rows padded to a multiple of 4 words (16-byte loads).  A CTA owns G
-// ciphertexts and walks the (i, j) pairs once; every thread holds four
-// output coefficients of all G ciphertexts in registers and loads the
-// base-1 non-zero rows of each (i, j) once for the whole group, so each
-// table row read from L2 serves G ciphertexts.  The table (62 MB for the
-// default set) stays L2-resident across the CTAs of a launch.
+// ciphertexts; each thread owns four output coefficients (one 16-byte
+// column) of all G of them, in registers.  The CTA walks the (i, j) pairs
+// once: for four levels j at a time it loads the base-1 non-zero rows of each
+// level (independent 16-byte loads, coalesced across the warp), then applies
+// them to its G ciphertexts.  The digits are computed once per CTA in the
+// prologue (8 digits of 2 bits packed per coefficient in shared memory), so a
+// digit costs a shift and a mask; it is the same for every lane of a warp,
+// so the row choice is a warp-uniform branch.  Each table row read from L2
+// serves G ciphertexts; the table (62 MB for the default set) stays
+// L2-resident across the CTAs of a launch.
 #include "engine.h"
 
 namespace tfhe_gb300 {
 
 namespace {
 
-constexpr int kKsGroup = 8;      // ciphertexts per CTA
-constexpr int kKsMaxBase = 4;    // basebit <= 2
+constexpr int kKsGroup = 8;  // ciphertexts per CTA
+constexpr int kKsJBlock = 4; // digit levels loaded together
 
-__global__ void __launch_bounds__(256) k_keyswitch(const int32_t* __restrict__ ks, int row_stride,
-                                                   const int32_t* __restrict__ in,
-                                                   int32_t* __restrict__ out, int count, int n,
-                                                   int n_in, int t, int basebit) {
-    extern __shared__ __align__(16) uint32_t s_in[];  // kKsGroup x (n_in + 1)
+__device__ __forceinline__ void sub4(uint4& a, const uint4& r) {
+    a.x -= r.x;
+    a.y -= r.y;
+    a.z -= r.z;
+    a.w -= r.w;
+}
+
+// basebit = 2 (base 4), t a multiple of kKsJBlock and <= 16.
+__global__ void __launch_bounds__(160) k_keyswitch_b4(const int32_t* __restrict__ ks, int row_stride,
+                                                      const int32_t* __restrict__ in,
+                                                      int32_t* __restrict__ out, int count, int n,
+                                                      int n_in, int t) {
+    extern __shared__ __align__(16) uint32_t s_dig[];  // kKsGroup x n_in packed digits
+    __shared__ uint32_t s_b[kKsGroup];
     const int c0 = blockIdx.x * kKsGroup;
     const int G = min(kKsGroup, count - c0);
     const int w_in = n_in + 1;
-    for (int i = threadIdx.x; i < G * w_in; i += blockDim.x)
-        s_in[i] = (uint32_t)in[(size_t)c0 * w_in + i];
+    const uint32_t prec_offset = 1u << (32 - (1 + 2 * t));
+    for (int idx = threadIdx.x; idx < G * n_in; idx += blockDim.x) {
+        const int g = idx / n_in, i = idx - g * n_in;
+        const uint32_t aibar = (uint32_t)in[(size_t)(c0 + g) * w_in + i] + prec_offset;
+        // digit j = (aibar >> (32 - 2(j+1))) & 3, packed at bits 2j
+        uint32_t packed = 0;
+        for (int j = 0; j < t; ++j) packed |= ((aibar >> (30 - 2 * j)) & 3u) << (2 * j);
+        s_dig[g * n_in + i] = packed;
+    }
+    if (threadIdx.x < G) s_b[threadIdx.x] = (uint32_t)in[(size_t)(c0 + threadIdx.x) * w_in + n_in];
     __syncthreads();
 
-    const int base = 1 << basebit;
-    const uint32_t mask = (uint32_t)base - 1;
-    const uint32_t prec_offset = 1u << (32 - (1 + basebit * t));
-    const int nvec = (n + 1 + 3) >> 2;  // int4 chunks of a row
+    const int nvec = (n + 1 + 3) >> 2;
     const int v = threadIdx.x;
     const bool live = v < nvec;
+    const int vv = live ? v : 0;  // idle lanes load a valid column and drop it
+    const int rs4 = row_stride >> 2;
 
     uint4 acc[kKsGroup];
 #pragma unroll
     for (int g = 0; g < kKsGroup; ++g) acc[g] = make_uint4(0, 0, 0, 0);
 
+    const int4* base = reinterpret_cast<const int4*>(ks);
+#pragma unroll 1
     for (int i = 0; i < n_in; ++i) {
-        for (int j = 0; j < t; ++j) {
-            const int shift = 32 - (j + 1) * basebit;
-            uint4 row[kKsMaxBase];
+#pragma unroll 1
+        for (int j0 = 0; j0 < t; j0 += kKsJBlock) {
+            uint4 row[kKsJBlock][3];
 #pragma unroll
-            for (int h = 0; h < kKsMaxBase; ++h) row[h] = make_uint4(0, 0, 0, 0);
-            if (live) {
-                const int4* rp =
-                    reinterpret_cast<const int4*>(ks + ((size_t)(i * t + j) * base) * row_stride);
+            for (int jj = 0; jj < kKsJBlock; ++jj) {
+                const int4* rp = base + ((size_t)(i * t + j0 + jj) * 4) * rs4 + vv;
 #pragma unroll
-                for (int h = 1; h < kKsMaxBase; ++h) {
-                    if (h < base) {
-                        const int4 r = __ldg(rp + (size_t)h * (row_stride >> 2) + v);
-                        row[h] = make_uint4((uint32_t)r.x, (uint32_t)r.y, (uint32_t)r.z,
-                                            (uint32_t)r.w);
-                    }
+                for (int h = 1; h < 4; ++h) {
+                    const int4 r = __ldg(rp + (size_t)h * rs4);
+                    row[jj][h - 1] = make_uint4((uint32_t)r.x, (uint32_t)r.y, (uint32_t)r.z,
+                                                (uint32_t)r.w);
                 }
             }
 #pragma unroll
             for (int g = 0; g < kKsGroup; ++g) {
                 if (g >= G) break;
-                const uint32_t aij = ((s_in[g * w_in + i] + prec_offset) >> shift) & mask;
+                const uint32_t dg = s_dig[g * n_in + i] >> (2 * j0);
 #pragma unroll
-                for (int h = 1; h < kKsMaxBase; ++h) {
-                    const uint32_t m = (aij == (uint32_t)h) ? 0xffffffffu : 0u;
-                    acc[g].x -= row[h].x & m;
-                    acc[g].y -= row[h].y & m;
-                    acc[g].z -= row[h].z & m;
-                    acc[g].w -= row[h].w & m;
+                for (int jj = 0; jj < kKsJBlock; ++jj) {
+                    switch ((dg >> (2 * jj)) & 3u) {
+                    case 1: sub4(acc[g], row[jj][0]); break;
+                    case 2: sub4(acc[g], row[jj][1]); break;
+                    case 3: sub4(acc[g], row[jj][2]); break;
+                    default: break;
+                    }
                 }
             }
         }
@@ -87,7 +107,7 @@ __global__ void __launch_bounds__(256) k_keyswitch(const int32_t* __restrict__ k
         for (int e = 0; e < 4; ++e) {
             const int q = 4 * v + e;
             if (q < n) o[q] = (int32_t)vals[e];
-            if (q == n) o[q] = (int32_t)(vals[e] + s_in[g * w_in + n_in]);
+            if (q == n) o[q] = (int32_t)(vals[e] + s_b[g]);
         }
     }
 }
@@ -97,19 +117,20 @@ __global__ void __launch_bounds__(256) k_keyswitch(const int32_t* __restrict__ k
 cudaError_t launch_keyswitch(const DevParams& P, const int32_t* ks, int32_t row_stride,
                              const int32_t* in, int32_t* out, int count, cudaStream_t st) {
     if (count <= 0) return cudaSuccess;
-    if (P.ks_basebit < 1 || P.ks_basebit > 2 || (row_stride & 3) || row_stride < P.n + 1)
+    if (P.ks_basebit != 2 || P.ks_t % kKsJBlock || P.ks_t > 16 || (row_stride & 3) ||
+        row_stride < P.n + 1)
         return cudaErrorInvalidValue;
     const int n_in = P.k * P.N;
     const int nvec = (P.n + 1 + 3) / 4;
     const int threads = ((nvec + 31) / 32) * 32;
-    if (threads > 256) return cudaErrorInvalidValue;
-    const size_t smem = (size_t)kKsGroup * (n_in + 1) * sizeof(uint32_t);
-    cudaError_t e = cudaFuncSetAttribute(k_keyswitch, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    if (threads > 160) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)kKsGroup * n_in * sizeof(uint32_t);
+    cudaError_t e = cudaFuncSetAttribute(k_keyswitch_b4,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int grid = (count + kKsGroup - 1) / kKsGroup;
-    k_keyswitch<<<grid, threads, smem, st>>>(ks, row_stride, in, out, count, P.n, n_in, P.ks_t,
-                                             P.ks_basebit);
+    k_keyswitch_b4<<<grid, threads, smem, st>>>(ks, row_stride, in, out, count, P.n, n_in,
+                                                P.ks_t);
     return cudaGetLastError();
 }
 

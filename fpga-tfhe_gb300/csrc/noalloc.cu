@@ -113,6 +113,7 @@ extern "C" tfhe_gpu_status tfhe_gpu_bootsGates_noalloc(tfhe_gpu_ctx* ctx, const 
     e = launch_gate_combine(ctx->dp, gates, 0, ca, cb, x, count, st);
     if (e != cudaSuccess) return cuda_error(ctx, e, "gate combination");
     EpArgs a{};
+    a.err = ctx->d_err;
     a.x = x;
     a.mu = tfhe_client_mod_switch_to_torus32(1, 8);
     a.lwe_out = u;

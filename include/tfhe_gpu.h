@@ -92,12 +92,22 @@ const char* tfhe_gpu_last_error(const tfhe_gpu_ctx* ctx);
 tfhe_gpu_status tfhe_gpu_get_params(const tfhe_gpu_ctx* ctx, tfhe_params* out);
 /* The context's own stream (as void*). */
 void* tfhe_gpu_stream(const tfhe_gpu_ctx* ctx);
-/* Wait for all work of the context's stream. */
+/* Wait for all work of the context's stream; TFHE_GPU_TIMEOUT if a kernel's
+ * bounded wait gave up since the last check. */
 tfhe_gpu_status tfhe_gpu_synchronize(tfhe_gpu_ctx* ctx);
 /* Bytes of one TGSW sample in the engine's transform layout. */
 size_t tfhe_gpu_tgsw_fft_bytes(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form);
 /* Device bytes the context holds (keys, tables, scratch). */
 size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
+
+/* Launch shape of the blind-rotation kernel of `form`: ciphertexts per CTA
+ * (64 threads each).  split-FP32: 4 or 6 = key rows read from L2 by every
+ * ciphertext; 5 or 8 = key rows streamed once per CTA into a shared-memory
+ * ring by a producer warp.  FP64: 3 (L2) or 4 (ring).  Engine tuning knob,
+ * no counterpart in the reference (its kernel is a single HLS work-item). */
+tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,
+                                            int32_t groups);
+int32_t tfhe_gpu_get_groups_per_cta(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form);
 
 /* ---- keys --------------------------------------------------------------- */
 

@@ -81,7 +81,8 @@ def test_stress_set_keygen_matches_oracle(pkg, oracle):
 def test_create_rejects_bad_params_without_gpu(pkg):
     lib = pkg.lib()
     h = ctypes.c_void_p()
-    for field, value in (("N", 2048), ("k", 2), ("Bgbit", 0), ("ks_basebit", 3), ("split_bits", 40)):
+    for field, value in (("N", 2048), ("k", 2), ("Bgbit", 0), ("ks_basebit", 3), ("ks_t", 6),
+                         ("l", 4), ("split_bits", 40)):
         P = pkg.default_params()
         setattr(P, field, value)
         assert lib.tfhe_gpu_create(ctypes.byref(P), 0, ctypes.byref(h)) == 1  # BAD_PARAM

@@ -223,3 +223,34 @@ def test_errors_are_status_codes(pkg, keys, torch_cuda, P):
         e.synchronize()
     finally:
         e.close()
+
+
+@pytest.mark.parametrize("form,groups", [("split_fp32", 4), ("split_fp32", 5), ("split_fp32", 6),
+                                         ("split_fp32", 8), ("fp64", 3), ("fp64", 4)])
+def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, groups):
+    """Each blind-rotation launch shape (L2-direct and shared-ring kernels) on
+    a ragged batch: decrypted bits equal the truth and the oracle's, phases
+    within tolerance, no device timeout."""
+    torch = torch_cuda
+    a, b, ca, cb = inputs
+    count = 37  # not a multiple of any group count: the last CTA is partial
+    e = pkg.Engine(pkg.default_params())
+    try:
+        e.upload_bootstrapping_key(keys["bk"], forms=(form,))
+        e.upload_keyswitch_key(keys["ks"])
+        e.set_groups_per_cta(form, groups)
+        gates = np.arange(count, dtype=np.int32) % 10
+        d_out = torch.zeros((count, P.n + 1), dtype=torch.int32, device="cuda")
+        e.bootsGates(dev(torch, gates), d_out, dev(torch, ca[:count]), dev(torch, cb[:count]), count,
+                     form, stream=cur(torch))
+        torch.cuda.synchronize()
+        e.synchronize()  # raises on a device-side timeout
+        got = host(d_out)
+    finally:
+        e.close()
+    names = sorted(pyoracle.GATES, key=lambda g: pyoracle.GATES[g])
+    truth = np.array([pyoracle.GATE_FN[names[g]](x, y) for g, x, y in zip(gates, a[:count], b[:count])])
+    assert (oracle.decrypt_bits(P, got, keys["lwe"]) == truth).all()
+    ref = oracle.boots_gate_batch(P, keys["bk_fft"], keys["ks"], gates[:4], ca[:4], cb[:4])
+    d = wrap_diff(oracle.phases(got[:4], keys["lwe"], P.n), oracle.phases(ref, keys["lwe"], P.n))
+    assert np.abs(d).max() <= PHASE_TOL
