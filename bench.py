@@ -232,7 +232,7 @@ def main():
     eng.upload_bootstrapping_key(bk, forms=("fp64", "split_fp32"))
     eng.upload_keyswitch_key(ks)
     if args.groups:
-        eng.set_groups_per_cta("split_fp32", args.groups)
+        eng.set_groups_per_cta(args.form, args.groups)
     batch = args.batch
     a, b, gates, ca, cb = make_inputs(pkg, P, lwe, batch)
     dev = torch.device("cuda", local)

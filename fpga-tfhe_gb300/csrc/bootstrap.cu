@@ -185,7 +185,7 @@ __device__ __forceinline__ void mac_row(cpx<R> (&out)[2][PARTS][8], const cpx<R>
 }
 
 template <typename R, int PARTS, bool ROT, int L, int FB, int IB, int NB, typename Keys>
-__device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, const Keys& keys, int a) {
+__device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& keys, int a) {
     static_assert(L % FB == 0 && PARTS % IB == 0 && FB <= NB && IB <= NB, "batch sizes");
     const int t = S.t;
     const int halfBg = 1 << (S.Bgbit - 1);
@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(64 * GROUPS, 1) k_external_product(KParams kp,
             const int ai = a_next;
             if (i + 1 < n) a_next = bara ? bara[i + 1] : mod_switch_2n(xs[i + 1]);
             if (ai == 0) continue;  // tfhe_blindRotate_FFT.cpp:114
-            const GlobalKeys<R, PARTS> keys{gsw_base + (size_t)i * gsw_elems};
+            GlobalKeys<R, PARTS> keys{gsw_base + (size_t)i * gsw_elems};
             ep_step<R, PARTS, true, L, L, PARTS, NB>(S, keys, ai);
         }
         if (a.acc_out) {
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(64 * GROUPS, 1) k_external_product(KParams kp,
         group_sync(S.bar_id);
         const cpx<R>* gsw = reinterpret_cast<const cpx<R>*>(
             reinterpret_cast<const char*>(a.gsw) + a.gsw_stride * (size_t)c);
-        const GlobalKeys<R, PARTS> keys{gsw};
+        GlobalKeys<R, PARTS> keys{gsw};
         if (MODE == kEpPlain) {
             ep_step<R, PARTS, false, L, L, PARTS, NB>(S, keys, 0);
         } else {
@@ -406,15 +406,52 @@ __global__ void __launch_bounds__(64 * GROUPS, 1) k_external_product(KParams kp,
 template <typename R, int PARTS, int S>
 struct RingKeys {
     static constexpr size_t kRow = (size_t)2 * PARTS * kHalf;
+    static constexpr size_t kRowBytes = kRow * sizeof(cpx<R>);
     static constexpr bool kShared = true;
-    const cpx<R>* ring;
+    cpx<R>* ring;
     uint64_t* full;
     uint64_t* empty;
     uint32_t row0;
     int32_t* err;
+    // In-line producer (one thread of the CTA when there is no producer
+    // warp): before taking row r it issues rows up to r + S - 1, waiting only
+    // for rows it needs itself (<= r) and skipping ahead rows whose slot is
+    // still held.
+    bool producer;
+    const char* src;       // key rows in global memory
+    uint32_t total;        // rows to stream
+    uint32_t next_issue;   // first row not issued yet
+
+    __device__ __forceinline__ void issue_upto(uint32_t r) {
+        while (next_issue < total && next_issue < r + S) {
+            const uint32_t slot = next_issue % S;
+            if (next_issue >= S) {
+                const uint32_t parity = ((next_issue / S) - 1) & 1;
+                if (next_issue <= r) {
+                    if (!mbar_wait_bounded(&empty[slot], parity)) {
+                        atomicExch(err, 3);
+                        next_issue = total;  // stop streaming; consumers time out and finish
+                        return;
+                    }
+                } else if (!mbar_try_wait(&empty[slot], parity)) {
+                    return;
+                }
+            }
+            mbar_arrive_expect_tx(&full[slot], (uint32_t)kRowBytes);
+            bulk_copy_g2s(reinterpret_cast<char*>(ring) + slot * kRowBytes,
+                          src + (size_t)next_issue * kRowBytes, (uint32_t)kRowBytes, &full[slot]);
+            ++next_issue;
+        }
+    }
+    // wait until every issued copy has landed (end of kernel)
+    __device__ __forceinline__ void drain() {
+        for (uint32_t r = next_issue > S ? next_issue - S : 0; r < next_issue; ++r)
+            if (!mbar_wait_bounded(&full[r % S], (r / S) & 1)) atomicExch(err, 3);
+    }
     __device__ __forceinline__ void prefetch(int, int, int) const {}
-    __device__ __forceinline__ const cpx<R>* acquire(int p) const {
+    __device__ __forceinline__ const cpx<R>* acquire(int p) {
         const uint32_t r = row0 + (uint32_t)p;
+        if (producer) issue_upto(r);
         const uint32_t slot = r % S;
         if (!mbar_wait_bounded(&full[slot], (r / S) & 1)) atomicExch(err, 3);
         return ring + slot * kRow;
@@ -434,8 +471,8 @@ struct RingPlan {
     static constexpr size_t total = group_off + GROUPS * group;
 };
 
-template <typename R, int PARTS, int GROUPS, int L, int S>
-__global__ void __launch_bounds__(64 * GROUPS + 32, 1)
+template <typename R, int PARTS, int GROUPS, int L, int S, bool INLINE>
+__global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
     k_blind_rotate_ring(KParams kp, Tables T, EpArgs a) {
     using Plan = RingPlan<R, PARTS, GROUPS, L, S>;
     constexpr int kpl = 2 * L;
@@ -457,27 +494,17 @@ __global__ void __launch_bounds__(64 * GROUPS + 32, 1)
 
     const int warp = threadIdx.x >> 5;
     const int n = kp.n;
-    if (warp == 2 * GROUPS) {
+    const uint32_t total_rows = (uint32_t)n * kpl;
+    RingKeys<R, PARTS, S> keys{ring, full, empty, 0, a.err, false,
+                               reinterpret_cast<const char*>(a.gsw), total_rows, 0};
+    if (!INLINE && warp == 2 * GROUPS) {
         // producer warp: one lane streams all n * 2l key rows in order
         if ((threadIdx.x & 31) == 0) {
-            const char* src = reinterpret_cast<const char*>(a.gsw);
-            const uint32_t total = (uint32_t)n * kpl;
-            uint32_t issued = 0;
-            for (uint32_t r = 0; r < total; ++r) {
-                const uint32_t slot = r % S;
-                if (r >= S && !mbar_wait_bounded(&empty[slot], ((r / S) - 1) & 1)) {
-                    atomicExch(a.err, 3);
-                    break;
-                }
-                mbar_arrive_expect_tx(&full[slot], (uint32_t)Plan::kRowBytes);
-                bulk_copy_g2s(reinterpret_cast<char*>(ring) + slot * Plan::kRowBytes,
-                              src + (size_t)r * Plan::kRowBytes, (uint32_t)Plan::kRowBytes,
-                              &full[slot]);
-                issued = r + 1;
+            for (uint32_t r = 0; r < total_rows; ++r) {
+                keys.issue_upto(r);  // blocks on row r's slot, issues up to r + S - 1
+                if (keys.next_issue <= r) break;  // timed out
             }
-            // do not leave the CTA with copies still landing in its memory
-            for (uint32_t r = issued > S ? issued - S : 0; r < issued; ++r)
-                if (!mbar_wait_bounded(&full[r % S], (r / S) & 1)) atomicExch(a.err, 3);
+            keys.drain();
         }
         return;
     }
@@ -486,6 +513,7 @@ __global__ void __launch_bounds__(64 * GROUPS + 32, 1)
     const int t = threadIdx.x & 63;
     const int c = blockIdx.x * GROUPS + g;
     if (g >= active) return;
+    keys.producer = INLINE && threadIdx.x == 0;
 
     char* gbase = smem + Plan::group_off + (size_t)g * Plan::group;
     StepCtx<R, PARTS, 1> St;
@@ -513,7 +541,6 @@ __global__ void __launch_bounds__(64 * GROUPS + 32, 1)
     group_sync(St.bar_id);
     const int32_t* bara = a.bara ? a.bara + (size_t)c * n : nullptr;
     const int32_t* xs = a.x ? a.x + (size_t)c * (n + 1) : nullptr;
-    RingKeys<R, PARTS, S> keys{ring, full, empty, 0, a.err};
     int a_next = bara ? bara[0] : mod_switch_2n(xs[0]);
 #pragma unroll 1
     for (int i = 0; i < n; ++i) {
@@ -529,6 +556,7 @@ __global__ void __launch_bounds__(64 * GROUPS + 32, 1)
         }
         ep_step<R, PARTS, true, L, 1, 1, 1>(St, keys, ai);
     }
+    if (keys.producer) keys.drain();
     if (a.acc_out) {
         int32_t* dst = a.acc_out + (size_t)c * 2 * kN;
         for (int i = t; i < 2 * kN; i += 64) dst[i] = St.acc[i];
@@ -853,7 +881,7 @@ cudaError_t launch_ep_t(const DevParams& P, const Tables& T, const EpArgs& a, cu
     return cudaGetLastError();
 }
 
-template <typename R, int PARTS, int GROUPS, int L>
+template <typename R, int PARTS, int GROUPS, int L, bool INLINE>
 cudaError_t launch_ring_t(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
     constexpr int S = 4;
     if (a.count <= 0) return cudaSuccess;
@@ -863,11 +891,11 @@ cudaError_t launch_ring_t(const DevParams& P, const Tables& T, const EpArgs& a, 
     kp.split = P.split_bits;
     kp.offset = decomp_offset(P.l, P.Bgbit);
     using Plan = RingPlan<R, PARTS, GROUPS, L, S>;
-    auto kern = k_blind_rotate_ring<R, PARTS, GROUPS, L, S>;
+    auto kern = k_blind_rotate_ring<R, PARTS, GROUPS, L, S, INLINE>;
     cudaError_t e = set_smem(kern, Plan::total);
     if (e != cudaSuccess) return e;
     const int grid = (a.count + GROUPS - 1) / GROUPS;
-    kern<<<grid, 64 * GROUPS + 32, Plan::total, st>>>(kp, T, a);
+    kern<<<grid, 64 * GROUPS + (INLINE ? 0 : 32), Plan::total, st>>>(kp, T, a);
     return cudaGetLastError();
 }
 
@@ -882,18 +910,18 @@ cudaError_t launch_ep_l(const DevParams& P, Form f, EpMode mode, const Tables& T
         case kEpMuxRotate: return launch_ep_t<double, 1, kEpMuxRotate, 3, L>(P, T, a, st);
         default:
             if (groups == 3) return launch_ep_t<double, 1, kEpBlindRotate, 3, L>(P, T, a, st);
-            return launch_ring_t<double, 1, 4, L>(P, T, a, st);
+            return launch_ring_t<double, 1, 4, L, true>(P, T, a, st);
         }
     }
     switch (mode) {
     case kEpPlain: return launch_ep_t<float, 2, kEpPlain, 4, L>(P, T, a, st);
     case kEpMuxRotate: return launch_ep_t<float, 2, kEpMuxRotate, 4, L>(P, T, a, st);
     default:
-        // groups 4 / 6: the L2-direct kernel; 5 / 8: the shared-ring kernel
+        // 4: L2-direct key reads; 5: shared ring fed by a producer warp;
+        // 6: shared ring fed in line by one consumer thread
         if (groups == 4) return launch_ep_t<float, 2, kEpBlindRotate, 4, L>(P, T, a, st);
-        if (groups == 6) return launch_ep_t<float, 2, kEpBlindRotate, 6, L>(P, T, a, st);
-        if (groups == 8) return launch_ring_t<float, 2, 8, L>(P, T, a, st);
-        return launch_ring_t<float, 2, 5, L>(P, T, a, st);
+        if (groups == 5) return launch_ring_t<float, 2, 5, L, false>(P, T, a, st);
+        return launch_ring_t<float, 2, 6, L, true>(P, T, a, st);
     }
 }
 

@@ -101,9 +101,10 @@ size_t tfhe_gpu_tgsw_fft_bytes(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form);
 size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
 
 /* Launch shape of the blind-rotation kernel of `form`: ciphertexts per CTA
- * (64 threads each).  split-FP32: 4 or 6 = key rows read from L2 by every
- * ciphertext; 5 or 8 = key rows streamed once per CTA into a shared-memory
- * ring by a producer warp.  FP64: 3 (L2) or 4 (ring).  Engine tuning knob,
+ * (64 threads each).  split-FP32: 4 = key rows read from L2 by every
+ * ciphertext; 5 = key rows streamed once per CTA into a shared-memory ring by
+ * a producer warp; 6 = the same ring fed by one consumer thread in line.
+ * FP64: 3 (L2) or 4 (ring, in line).  Engine tuning knob,
  * no counterpart in the reference (its kernel is a single HLS work-item). */
 tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,
                                             int32_t groups);
