@@ -12,11 +12,14 @@
  * exist only upstream restate the published TFHE algorithm (Chillotti, Gama,
  * Georgieva, Izabachene, J. Cryptology 2020) and say so.
  *
- * Parity pins: see tests/test_oracle_pins.py (known answers taken from the
- * reference: mu = modSwitchToTorus32(1,8) = 2^29, the offset 2164391936,
- * the 16-bit OR of 499 and 388 from test_bench/, exact integer semantics)
- * and oracle/ref_pin/ (the reference's own sources compiled against a
- * header shim and compared function by function).
+ * Parity pins: tests/test_oracle_vs_reference.py compares this restatement
+ * function by function with the reference's own sources compiled on the CPU
+ * (oracle/ref_pin/build_ref.py -> oracle/_ref/): bit-exact for the integer
+ * functions, RNG and key switch, within 1-2 units for the FFT path.
+ * tests/test_oracle_pins.py holds the known answers (mu = 2^29, the offset
+ * 2164391936, 499 OR 388 = 503 from test_bench/).  The upstream-only pieces
+ * (TLWE/TGSW keygen, extraction, gate constants other than OR) are not
+ * pinned: the upstream library is absent.
  *
  * Layouts (all int32 arrays are Torus32 values, arithmetic mod 2^32):
  *   LWE sample         : int32[n + 1]            a[0..n-1], b
