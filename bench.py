@@ -58,6 +58,15 @@ def parse():
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--form", default="split_fp32", choices=["split_fp32", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--workload", default="layer",
+                    choices=["layer", "extprod", "stress", "failures", "serve"],
+                    help="layer: 4096-gate circuit layer (default, the headline); extprod: 1024 "
+                         "external products; stress: 65536 NAND on the n=500/l=2/Bgbit=10 set; "
+                         "failures: 10^6 gates as chained layers, decryption checked; serve: "
+                         "64 Poisson clients submitting circuits to the continuous-batching server")
+    ap.add_argument("--clients", type=int, default=64)
+    ap.add_argument("--requests", type=int, default=8, help="requests per client (serve)")
+    ap.add_argument("--rate", type=float, default=8.0, help="requests/s per client (serve)")
     ap.add_argument("--groups", type=int, default=0,
                     help="ciphertexts per CTA of the split-FP32 blind rotation (0 = engine default)")
     ap.add_argument("--no-extras", action="store_true",
@@ -211,11 +220,342 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# side workloads (one JSON line each; the default run is the layer above)
+# ---------------------------------------------------------------------------
+def _engine_setup(P, seed, local, forms=("fp64", "split_fp32")):
+    import torch
+    import __graft_entry__ as ge
+    torch.cuda.set_device(local)
+    ge.build()
+    pkg = ge.load_package()
+    lwe, tlwe, ks, bk = pkg.gate_keyset(P, seed)
+    eng = pkg.Engine(P, device=local)
+    eng.upload_bootstrapping_key(bk, forms=forms)
+    eng.upload_keyswitch_key(ks)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    return torch, pkg, eng, (lwe, tlwe, ks, bk), stream
+
+
+def _time_steps(torch, stream, fn, steps, warmup, flush=None):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ms = []
+    for s in range(steps):
+        if flush is not None:
+            flush.fill_(s)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return ms
+
+
+def workload_extprod(args, world, rank, local):
+    """1024 independent TGSW x TRLWE products (tGswFFTExternMulToTLwe):
+    TRLWE coefficients uniform int32 (numpy seed 2), TGSW = encryption of X^e,
+    e uniform in [0, 2N) (seed 3), checked against the exact int64 product.
+    Roofline: HBM (each product reads its own 98,304-byte TGSW)."""
+    from oracle import pyoracle
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    P = pkg.default_params()
+    torch, pkg, eng, keys, stream = _engine_setup(P, [0], local, forms=("fp64",))
+    lwe, tlwe, ks, bk = keys
+    count = 1024
+    o = pyoracle.get()
+    OP = pyoracle.default_params()
+    rng = np.random.default_rng(2)
+    acc = rng.integers(-2 ** 31, 2 ** 31, (count, 2 * P.N)).astype(np.int32)
+    es = np.random.default_rng(3).integers(0, 2 * P.N, count)
+    # TGSW(X^e): one encryption of 1 per 16 products, rows rotated by X^e
+    o.set_seed([3])
+    base = [o.tgsw_encrypt_int(OP, 1, OP.tlwe_alpha, tlwe).reshape(OP.kpl, 2, P.N) for _ in range(16)]
+    gsw = np.empty((count, OP.kpl * 2 * P.N), np.int32)
+    for c in range(count):
+        g = base[c % 16]
+        gsw[c] = np.stack([[o.mul_by_xai(P.N, int(es[c]), g[p, j]) for j in range(2)]
+                           for p in range(OP.kpl)]).reshape(-1)
+    sp = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    d_gsw_time = torch.from_numpy(gsw).cuda()
+    d_acc0 = torch.from_numpy(acc).cuda()
+    res = {}
+    for form in ("fp64", "split_fp32"):
+        nb = eng.tgsw_fft_bytes(form)
+        d_g = torch.empty(count * nb, dtype=torch.uint8, device="cuda")
+        eng.tgsw_to_fft(d_gsw_time, d_g, count, form, stream=sp)
+        d_acc = d_acc0.clone()
+        # the product's work does not depend on the values: time it in place
+        ms = _time_steps(torch, stream,
+                         lambda: eng.tGswFFTExternMulToTLwe(d_acc, d_g, count, form, stream=sp),
+                         args.steps, args.warmup, flush)
+        kms = statistics.median(ms)
+        d_acc.copy_(d_acc0)
+        eng.tGswFFTExternMulToTLwe(d_acc, d_g, count, form, stream=sp)
+        torch.cuda.synchronize()
+        got = d_acc.cpu().numpy()
+        errs = []
+        for c in range(0, count, 128):
+            ex = o.extern_mul_exact(OP, acc[c], gsw[c]).astype(np.int64)
+            d = (got[c].astype(np.int64) - ex + 2 ** 31) % 2 ** 32 - 2 ** 31
+            errs.append(np.abs(d).max())
+        bytes_per = nb + 2 * 2 * P.N * 4
+        res[form] = {"products_per_s": count / (kms / 1000.0), "kernel_ms": kms,
+                     "hbm_gbs": count * bytes_per / (kms / 1000.0) / 1e9,
+                     "max_abs_err_vs_int64_units": int(max(errs))}
+    peak = _measured_peak("hbm_gbs")
+    f = res["split_fp32"]
+    line = {"metric": "external products/sec", "value": f["products_per_s"], "unit": "products/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": f["kernel_ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "1024 independent TGSW x TRLWE external products, N=1024, k=1, l=3, "
+                                   "Bgbit=7; TRLWE uniform int32 (seed 2), TGSW = encryption of X^e "
+                                   "(seed 3); L2 flushed between steps", "batch": count},
+            "forms": res,
+            "roofline": {"bound": "hbm", "achieved": f["hbm_gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": f["hbm_gbs"] / peak if peak else None, "traffic": None,
+                         "algorithmic_bytes_per_unit": eng.tgsw_fft_bytes("split_fp32") + 16384,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs"}}
+    print(json.dumps(line), flush=True)
+
+
+def _measured_peak(key):
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)[key])
+    except (OSError, KeyError, ValueError):
+        return 6800.0 if key == "hbm_gbs" else None
+
+
+def workload_stress(args, world, rank, local):
+    """65536 NAND bootstraps on the alternative set n=500, l=2, Bgbit=10,
+    LWE 2^-15, TRLWE 2^-24: split-FP32 vs FP64, failure count, output phase
+    error, and the deviation from the exact int64 blind rotation on a sample."""
+    from oracle import pyoracle
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    P = pkg.stress_params()
+    torch, pkg, eng, keys, stream = _engine_setup(P, [0], local)
+    lwe, tlwe, ks, bk = keys
+    total = 65536
+    batch = 8192
+    rng = np.random.default_rng(4)
+    a = rng.integers(0, 2, total)
+    b = rng.integers(0, 2, total)
+    pkg.set_seed([4])
+    ca = pkg.encrypt_bits(P, a, lwe)
+    cb = pkg.encrypt_bits(P, b, lwe)
+    truth = 1 - (a & b)
+    sp = stream.cuda_stream
+    d_ca = torch.from_numpy(ca).cuda()
+    d_cb = torch.from_numpy(cb).cuda()
+    d_out = torch.empty_like(d_ca)
+    mu = 2 ** 29
+    res = {}
+    for form in ("split_fp32", "fp64"):
+        def run_all():
+            for s0 in range(0, total, batch):
+                eng.bootsGate("NAND", d_out[s0:s0 + batch], d_ca[s0:s0 + batch], d_cb[s0:s0 + batch],
+                              batch, form, stream=sp)
+        ms = _time_steps(torch, stream, run_all, 1, 1)
+        out = d_out.cpu().numpy()
+        bits = pkg.decrypt_bits(P, out, lwe)
+        ph = pkg.phases(out, lwe).astype(np.int64)
+        err = np.abs(np.abs(ph) - mu) / 2.0 ** 32
+        res[form] = {"bootstraps_per_s": total / (ms[0] / 1000.0), "failures": int((bits != truth).sum()),
+                     "gates": total, "phase_err_max_turn": float(err.max()),
+                     "phase_err_mean_turn": float(err.mean()), "phase_err_std_turn": float(err.std())}
+    # deviation of the blind rotation (phase of the extracted sample under the
+    # TLWE key) from the exact int64 oracle on a few gates
+    o = pyoracle.get()
+    OP = pyoracle.stress_params()
+    sample = 2
+    xs = np.stack([o.gate_combine(OP, "NAND", ca[i], cb[i]) for i in range(sample)])
+    d_u = torch.empty((sample, P.N + 1), dtype=torch.int32, device="cuda")
+    dev_exact = {}
+    exact = [o.bootstrap_woks(OP, None, mu, xs[i], exact_bk=bk) for i in range(sample)]
+    ex_ph = np.array([o.phases(e, tlwe, P.N)[0] for e in exact], np.int64)
+    for form in ("split_fp32", "fp64"):
+        eng.tfhe_bootstrap_woKS_FFT(d_u, torch.from_numpy(xs).cuda(), mu, sample, form, stream=sp)
+        torch.cuda.synchronize()
+        u = d_u.cpu().numpy()
+        ph = np.array([o.phases(u[i], tlwe, P.N)[0] for i in range(sample)], np.int64)
+        dev_exact[form] = float(np.abs((ph - ex_ph + 2 ** 31) % 2 ** 32 - 2 ** 31).max() / 2.0 ** 32)
+        res[form]["phase_dev_vs_int64_turn_max"] = dev_exact[form]
+    f = res["split_fp32"]
+    line = {"metric": "gate bootstraps/sec", "value": f["bootstraps_per_s"], "unit": "bootstraps/s",
+            "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": total / f["bootstraps_per_s"] * 1000,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "precision stress: 65536 NAND bootstraps, n=500, N=1024, k=1, l=2, "
+                                   "Bgbit=10, ks t=8 basebit=2, LWE 2^-15, TRLWE 2^-24 (keys seed 0, "
+                                   "inputs seed 4)", "batch": batch, "split_bits": eng.params.split_bits},
+            "forms": res}
+    print(json.dumps(line), flush=True)
+
+
+def workload_failures(args, world, rank, local):
+    """10^6 gate bootstraps (default set, split-FP32) as 245 chained layers of
+    4096 random gates with random wiring: each layer's inputs are outputs of
+    the previous layer; every output decrypted and compared with plaintext
+    evaluation of the same circuit."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    P = pkg.default_params()
+    torch, pkg, eng, keys, stream = _engine_setup(P, [0], local, forms=("split_fp32",))
+    lwe = keys[0]
+    width, layers = 4096, 245
+    rng = np.random.default_rng(7)
+    bits = rng.integers(0, 2, width)
+    pkg.set_seed([7])
+    cur = torch.from_numpy(pkg.encrypt_bits(P, bits, lwe)).cuda()
+    sp = stream.cuda_stream
+    out = torch.empty_like(cur)
+    fns = [lambda x, y: 1 - (x & y), lambda x, y: x & y, lambda x, y: x | y, lambda x, y: x ^ y,
+           lambda x, y: 1 - (x ^ y), lambda x, y: 1 - (x | y), lambda x, y: (1 - x) & y,
+           lambda x, y: x & (1 - y), lambda x, y: (1 - x) | y, lambda x, y: x | (1 - y)]
+    failures = 0
+    worst = 0.0
+    t0 = time.perf_counter()
+    gpu_ms = 0.0
+    for layer in range(layers):
+        ia = rng.integers(0, width, width)
+        ib = rng.integers(0, width, width)
+        g = rng.integers(0, 10, width).astype(np.int32)
+        ca = cur[torch.from_numpy(ia).cuda()].contiguous()
+        cb = cur[torch.from_numpy(ib).cuda()].contiguous()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.bootsGates(torch.from_numpy(g).cuda(), out, ca, cb, width, "split_fp32", stream=sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        gpu_ms += e0.elapsed_time(e1)
+        nb = np.array([fns[gi](bits[x], bits[y]) for gi, x, y in zip(g, ia, ib)])
+        host = out.cpu().numpy()
+        got = pkg.decrypt_bits(P, host, lwe)
+        failures += int((got != nb).sum())
+        ph = pkg.phases(host, lwe).astype(np.int64)
+        worst = max(worst, float(np.abs(np.abs(ph) - 2 ** 29).max() / 2.0 ** 32))
+        bits = nb  # continue from the plaintext truth; the ciphertexts carry on
+        cur, out = out, cur
+    total = width * layers
+    line = {"metric": "decryption failures", "value": failures, "unit": "failures",
+            "gates": total, "n_gpus": 1, "steps": layers, "warmup": 0,
+            "ms_per_step": gpu_ms / layers, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "%d gate bootstraps: %d chained layers of %d random gates (all 10 "
+                                   "gate types, random wiring, seed 7), default set, split-FP32"
+                                   % (total, layers, width)},
+            "bootstraps_per_s": total / (gpu_ms / 1000.0),
+            "worst_phase_error_turn": worst, "wall_s": time.perf_counter() - t0}
+    print(json.dumps(line), flush=True)
+
+
+def workload_serve(args, world, rank, local):
+    """Serving: `clients` simulated clients, Poisson arrivals (rate per
+    client, seed 5), each request a random circuit -- 32-bit ripple-carry
+    adder (157 gates, depth 64), 16-bit comparator (cloud.c's compare_bit
+    chain, 16 XNOR + 16 MUX), 8-bit multiplexer (8 MUX) -- with random
+    operands, submitted to the continuous-batching server under one cloud
+    key.  Per-gate latency = gate ready -> bootstrapped; request latency =
+    arrival -> outputs back on the host.  Every output is decrypted and
+    checked."""
+    import importlib
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    P = pkg.default_params()
+    torch, pkg, eng, keys, stream = _engine_setup(P, [0], local)
+    circuits = importlib.import_module("tfhe_gb300.circuits")
+    lwe = keys[0]
+    rng = np.random.default_rng(5)
+    kinds = [("adder", circuits.ripple_carry_adder(32)), ("cmp", circuits.comparator(16)),
+             ("mux", circuits.multiplexer(8))]
+    reqs = []
+    pkg.set_seed([5])
+    for cl in range(args.clients):
+        t = 0.0
+        for _ in range(args.requests):
+            t += rng.exponential(1.0 / args.rate)
+            k = int(rng.integers(0, 3))
+            name, (gates, ni, outs) = kinds[k]
+            bits = rng.integers(0, 2, ni).astype(np.int32)
+            reqs.append({"t": t, "kind": name, "gates": gates, "ni": ni, "outs": outs,
+                         "ct": pkg.encrypt_bits(P, bits, lwe),
+                         "want": circuits.evaluate(gates, bits, outs)})
+    reqs.sort(key=lambda r: r["t"])
+    total_boots = sum(circuits.bootstraps(r["gates"]) for r in reqs)
+    result = {}
+    for form in ("split_fp32",):
+        srv = pkg.Server(eng, pool_slots=131072, max_batch=4096, form=form)
+        t0 = time.perf_counter()
+        nxt = 0
+        pending = {}
+        lat = {"adder": [], "cmp": [], "mux": []}
+        wrong = 0
+        while nxt < len(reqs) or pending:
+            now = time.perf_counter() - t0
+            while nxt < len(reqs) and reqs[nxt]["t"] <= now:
+                r = reqs[nxt]
+                pending[srv.submit(r["gates"], r["ni"], r["ct"], r["outs"])] = r
+                nxt += 1
+            ran = srv.step()
+            for rid in list(pending):
+                got = srv.poll(rid)
+                if got is not None:
+                    r = pending.pop(rid)
+                    lat[r["kind"]].append(time.perf_counter() - t0 - r["t"])  # from arrival
+                    wrong += int((pkg.decrypt_bits(P, got[0], lwe) != r["want"]).any())
+            if ran == 0 and not pending and nxt < len(reqs):
+                time.sleep(max(0.0, reqs[nxt]["t"] - (time.perf_counter() - t0)))
+        makespan = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        gl = np.array(st["gate_latency_s"]) * 1000
+        allr = np.concatenate([np.array(v) for v in lat.values() if v]) * 1000
+        result[form] = {
+            "bootstraps_per_s": total_boots / makespan, "makespan_s": makespan,
+            "busy_s": st["busy_s"], "bootstraps_per_busy_s": total_boots / st["busy_s"],
+            "gate_latency_ms": {"p50": float(np.percentile(gl, 50)), "p99": float(np.percentile(gl, 99))},
+            "request_latency_ms": {"p50": float(np.percentile(allr, 50)), "p99": float(np.percentile(allr, 99))},
+            "request_latency_ms_by_circuit": {k: {"p50": float(np.percentile(np.array(v) * 1000, 50)),
+                                                  "p99": float(np.percentile(np.array(v) * 1000, 99)),
+                                                  "n": len(v)} for k, v in lat.items() if v},
+            "requests": len(reqs), "wrong_requests": wrong}
+    f = result["split_fp32"]
+    line = {"metric": "gate bootstraps/sec (serving)", "value": f["bootstraps_per_s"],
+            "unit": "bootstraps/s", "n_gpus": 1, "steps": len(reqs), "warmup": 0,
+            "ms_per_step": f["makespan_s"] * 1000 / len(reqs), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "serving: %d clients x %d requests, Poisson arrivals %.1f req/s per "
+                                   "client (seed 5); circuits uniform over 32-bit ripple-carry adder, "
+                                   "16-bit comparator, 8-bit multiplexer; one cloud key; split-FP32; "
+                                   "%d bootstraps in total" % (args.clients, args.requests, args.rate,
+                                                               total_boots)},
+            "latency_ms": {"gate_p50": f["gate_latency_ms"]["p50"], "gate_p99": f["gate_latency_ms"]["p99"],
+                           "request_p50": f["request_latency_ms"]["p50"],
+                           "request_p99": f["request_latency_ms"]["p99"]},
+            "forms": result}
+    print(json.dumps(line), flush=True)
+
+
+WORKLOADS = {"extprod": workload_extprod, "stress": workload_stress, "failures": workload_failures,
+             "serve": workload_serve}
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload != "layer":
+        WORKLOADS[args.workload](args, world, rank, local)
         return
     import torch
     import __graft_entry__ as ge
@@ -354,6 +694,16 @@ def main():
             torch.cuda.synchronize()
             one_ms.append(e0.elapsed_time(e1))
         one = statistics.median(one_ms[1:])
+        one32 = []
+        for s in range(4):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.bootsGates(d_g, d_out, d_ca, d_cb, 1, "split_fp32", stream=sp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            one32.append(e0.elapsed_time(e1))
+        extras["split_fp32_single_gate_ms"] = statistics.median(one32[1:])
         extras["fp64_single_gate_ms"] = one
         extras["fp64_single_gate_bootstraps_per_s"] = 1000.0 / one
         extras["speedup_vs_fp64_single_gate"] = value / world / (1000.0 / one)

@@ -111,6 +111,16 @@ SIGNATURES = {
                                                 ctypes.c_int32, ctypes.c_int]),
     "tfhe_gpu_bootsGates_noalloc": (ctypes.c_int, [VP, VP, VP, VP, VP, ctypes.c_int32, ctypes.c_int,
                                                    VP]),
+    "tfhe_gpu_server_create": (ctypes.c_int, [VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int,
+                                               ctypes.POINTER(VP)]),
+    "tfhe_gpu_server_destroy": (None, [VP]),
+    "tfhe_gpu_server_last_error": (ctypes.c_char_p, [VP]),
+    "tfhe_gpu_server_submit": (ctypes.c_int, [VP, I32P, ctypes.c_int32, ctypes.c_int32, I32P, I32P,
+                                               ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]),
+    "tfhe_gpu_server_step": (ctypes.c_int, [VP, I32P]),
+    "tfhe_gpu_server_poll": (ctypes.c_int, [VP, ctypes.c_int64, I32P, I32P,
+                                             ctypes.POINTER(ctypes.c_double)]),
+    "tfhe_gpu_server_stats": (ctypes.c_int, [VP, F64P, F64P, F64P, ctypes.POINTER(ctypes.c_int64)]),
     "tfhe_client_set_seed": (None, [U32P, ctypes.c_int32]),
     "tfhe_client_gate_keyset": (ctypes.c_int, [ctypes.c_void_p, I32P, I32P, I32P, I32P]),
     "tfhe_client_encrypt_bits": (ctypes.c_int, [ctypes.c_void_p, I32P, ctypes.c_int32, I32P, I32P]),
@@ -382,3 +392,79 @@ class Engine:
                                                       ca.ctypes.data_as(I32P), cb.ctypes.data_as(I32P),
                                                       count, self._form(form)), "bootsGates_host")
         return out
+
+
+class Server:
+    """Continuous-batching gate server (tfhe_gpu_server_*) over an Engine."""
+
+    def __init__(self, engine, pool_slots=65536, max_batch=4096, form="split_fp32"):
+        self.engine = engine
+        self.lib = engine.lib
+        h = VP()
+        st = self.lib.tfhe_gpu_server_create(engine.ctx, int(pool_slots), int(max_batch),
+                                             engine._form(form), ctypes.byref(h))
+        if st:
+            raise TfheError(st, "tfhe_gpu_server_create")
+        self.srv = h
+        self.width = engine.params.n + 1
+        self.noutputs = {}
+
+    def close(self):
+        if getattr(self, "srv", None):
+            self.lib.tfhe_gpu_server_destroy(self.srv)
+            self.srv = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st:
+            raise TfheError(st, "%s: %s" % (what, self.lib.tfhe_gpu_server_last_error(self.srv).decode()))
+
+    def submit(self, gates, ninputs, inputs, outputs):
+        """gates: int32 [ngates, 4] (type, in0, in1, in2); inputs: int32
+        [ninputs, n+1]; outputs: wire ids.  Returns the request id."""
+        g = _np(gates, np.int32).reshape(-1, 4)
+        x = _np(inputs, np.int32).reshape(-1, self.width)
+        o = _np(outputs, np.int32)
+        rid = ctypes.c_int64()
+        self._check(self.lib.tfhe_gpu_server_submit(self.srv, g.ctypes.data_as(I32P), len(g), int(ninputs),
+                                                    x.ctypes.data_as(I32P), o.ctypes.data_as(I32P), len(o),
+                                                    ctypes.byref(rid)), "submit")
+        self.noutputs[rid.value] = len(o)
+        return rid.value
+
+    def step(self):
+        ran = ctypes.c_int32()
+        self._check(self.lib.tfhe_gpu_server_step(self.srv, ctypes.byref(ran)), "step")
+        return ran.value
+
+    def poll(self, rid):
+        """(outputs, latency_s) of a finished request, or None."""
+        out = np.zeros((self.noutputs[rid], self.width), np.int32)
+        done = ctypes.c_int32()
+        lat = ctypes.c_double()
+        self._check(self.lib.tfhe_gpu_server_poll(self.srv, int(rid), out.ctypes.data_as(I32P),
+                                                  ctypes.byref(done), ctypes.byref(lat)), "poll")
+        if not done.value:
+            return None
+        del self.noutputs[rid]
+        return out, lat.value
+
+    def stats(self):
+        st = np.zeros(8, np.float64)
+        cap = (ctypes.c_int64 * 2)(0, 0)
+        self._check(self.lib.tfhe_gpu_server_stats(self.srv, st.ctypes.data_as(F64P), None, None, cap),
+                    "stats")
+        g = np.zeros(max(cap[0], 1), np.float64)
+        r = np.zeros(max(cap[1], 1), np.float64)
+        self._check(self.lib.tfhe_gpu_server_stats(self.srv, st.ctypes.data_as(F64P), g.ctypes.data_as(F64P),
+                                                   r.ctypes.data_as(F64P), cap), "stats")
+        keys = ["queued", "active", "free_slots", "bootstraps", "busy_s", "n_gate_lat", "n_req_lat", "pool_slots"]
+        d = dict(zip(keys, st.tolist()))
+        d["gate_latency_s"] = g[:cap[0]]
+        d["request_latency_s"] = r[:cap[1]]
+        return d

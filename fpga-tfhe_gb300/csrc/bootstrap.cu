@@ -39,6 +39,7 @@ constexpr int kTabA = 0;
 constexpr int kTabB = 512;
 constexpr int kTabPsi = 576;
 constexpr int kTabSize = 1088;
+constexpr int kSmCount = 152;  // GB300
 
 // ----------------------------------------------------------------------
 // helpers
@@ -917,8 +918,20 @@ cudaError_t launch_ep_l(const DevParams& P, Form f, EpMode mode, const Tables& T
     case kEpPlain: return launch_ep_t<float, 2, kEpPlain, 4, L>(P, T, a, st);
     case kEpMuxRotate: return launch_ep_t<float, 2, kEpMuxRotate, 4, L>(P, T, a, st);
     default:
-        // 4: L2-direct key reads; 5: shared ring fed by a producer warp;
-        // 6: shared ring fed in line by one consumer thread
+        if (groups == 0) {
+            // automatic: a batch that fills every SM with 6 ciphertexts uses
+            // the shared-ring kernel; smaller batches are spread over more
+            // SMs (fewer ciphertexts per CTA, key rows from L2) for latency
+            const int per_sm = (a.count + kSmCount - 1) / kSmCount;
+            if (per_sm >= 6) return launch_ring_t<float, 2, 6, L, true>(P, T, a, st);
+            if (per_sm == 1) return launch_ep_t<float, 2, kEpBlindRotate, 1, L>(P, T, a, st);
+            if (per_sm == 2) return launch_ep_t<float, 2, kEpBlindRotate, 2, L>(P, T, a, st);
+            return launch_ep_t<float, 2, kEpBlindRotate, 4, L>(P, T, a, st);
+        }
+        // 1, 2, 4: L2-direct key reads; 5: shared ring fed by a producer
+        // warp; 6: shared ring fed in line by one consumer thread
+        if (groups == 1) return launch_ep_t<float, 2, kEpBlindRotate, 1, L>(P, T, a, st);
+        if (groups == 2) return launch_ep_t<float, 2, kEpBlindRotate, 2, L>(P, T, a, st);
         if (groups == 4) return launch_ep_t<float, 2, kEpBlindRotate, 4, L>(P, T, a, st);
         if (groups == 5) return launch_ring_t<float, 2, 5, L, false>(P, T, a, st);
         return launch_ring_t<float, 2, 6, L, true>(P, T, a, st);

@@ -101,10 +101,12 @@ size_t tfhe_gpu_tgsw_fft_bytes(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form);
 size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
 
 /* Launch shape of the blind-rotation kernel of `form`: ciphertexts per CTA
- * (64 threads each).  split-FP32: 4 = key rows read from L2 by every
- * ciphertext; 5 = key rows streamed once per CTA into a shared-memory ring by
- * a producer warp; 6 = the same ring fed by one consumer thread in line.
- * FP64: 3 (L2) or 4 (ring, in line).  Engine tuning knob,
+ * (64 threads each).  split-FP32: 0 = automatic (6 when the batch fills
+ * every SM six times over, else as few per CTA as spreads the batch over all
+ * SMs); 1, 2, 4 = key rows read from L2 by every ciphertext; 5 = key rows
+ * streamed once per CTA into a shared-memory ring by a producer warp; 6 = the
+ * same ring fed by one consumer thread in line.  FP64: 3 (L2) or 4 (ring,
+ * in line).  Engine tuning knob,
  * no counterpart in the reference (its kernel is a single HLS work-item). */
 tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,
                                             int32_t groups);
@@ -237,6 +239,41 @@ tfhe_gpu_status tfhe_gpu_bootsGates_noalloc(tfhe_gpu_ctx* ctx, const int32_t* ga
                                             int32_t* out, const int32_t* ca,
                                             const int32_t* cb, int32_t count,
                                             tfhe_gpu_form form, void* stream);
+
+/* ---- serving: continuous-batching gate server (test_bench/server/cloud.c) */
+/* The test_bench server runs one client's circuit gate by gate
+ * (cloud.c:9-36, 39-74).  The engine's server admits circuits from many
+ * clients into a device ciphertext pool of `pool_slots` slots (admission by
+ * device memory: a circuit waits until its wires fit), and each
+ * tfhe_gpu_server_step runs every ready gate of every admitted circuit as one
+ * batch (at most `max_batch` bootstraps), so requests that arrive while
+ * others run share their launches.  A circuit is a list of gates
+ * {type, in0, in1, in2}: types 0..9 as tfhe_gpu_gate, 10 = MUX (in0 ? in1 :
+ * in2), 11 = NOT, 12 = COPY, 13 = CONSTANT (in0 = the bit); wire ids
+ * [0, ninputs) are the inputs, ninputs + g the output of gate g, and a
+ * gate's inputs must be earlier wires. */
+typedef struct tfhe_gpu_server tfhe_gpu_server;
+tfhe_gpu_status tfhe_gpu_server_create(tfhe_gpu_ctx* ctx, int32_t pool_slots, int32_t max_batch,
+                                       tfhe_gpu_form form, tfhe_gpu_server** out);
+void tfhe_gpu_server_destroy(tfhe_gpu_server* srv);
+const char* tfhe_gpu_server_last_error(const tfhe_gpu_server* srv);
+/* Queue a circuit; input_ct is host int32[ninputs][n+1]. */
+tfhe_gpu_status tfhe_gpu_server_submit(tfhe_gpu_server* srv, const int32_t* gates, int32_t ngates,
+                                       int32_t ninputs, const int32_t* input_ct,
+                                       const int32_t* output_wires, int32_t noutputs,
+                                       int64_t* request_id);
+/* One tick: admit, run the ready gates as one batch, retire finished
+ * circuits; *ran = gates executed (0 when idle). */
+tfhe_gpu_status tfhe_gpu_server_step(tfhe_gpu_server* srv, int32_t* ran);
+/* Outputs of a finished request (host int32[noutputs][n+1]); *done = 0 while
+ * queued or running; latency from submission to completion in seconds. */
+tfhe_gpu_status tfhe_gpu_server_poll(tfhe_gpu_server* srv, int64_t request_id, int32_t* out,
+                                     int32_t* done, double* latency_s);
+/* stats[0..7]: queued, active, free slots, bootstraps run, busy seconds,
+ * gate latencies recorded, request latencies recorded, pool slots; gate
+ * (ready -> done) and request latencies copied up to cap[0], cap[1] entries. */
+tfhe_gpu_status tfhe_gpu_server_stats(tfhe_gpu_server* srv, double* stats, double* gate_lat,
+                                      double* req_lat, int64_t* cap);
 
 /* ---- client side (host): keygen, encryption, decryption --------------- */
 /* Exact semantics of the reference's numeric functions

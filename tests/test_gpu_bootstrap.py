@@ -225,7 +225,8 @@ def test_errors_are_status_codes(pkg, keys, torch_cuda, P):
         e.close()
 
 
-@pytest.mark.parametrize("form,groups", [("split_fp32", 4), ("split_fp32", 5), ("split_fp32", 6),
+@pytest.mark.parametrize("form,groups", [("split_fp32", 0), ("split_fp32", 1), ("split_fp32", 2),
+                                         ("split_fp32", 4), ("split_fp32", 5), ("split_fp32", 6),
                                          ("fp64", 3), ("fp64", 4)])
 def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, groups):
     """Each blind-rotation launch shape (L2-direct and shared-ring kernels) on
