@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--form", default="split_fp32", choices=["split_fp32", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
+    ap.add_argument("--serve-forms", default="split_fp32,fp64",
+                    help="transform forms the serving workload runs, in order")
+    ap.add_argument("--no-graph", action="store_true", help="launch the gate pipeline eagerly")
     ap.add_argument("--workload", default="layer",
                     choices=["layer", "extprod", "stress", "failures", "serve"],
                     help="layer: 4096-gate circuit layer (default, the headline); extprod: 1024 "
@@ -491,7 +495,7 @@ def workload_serve(args, world, rank, local):
     reqs.sort(key=lambda r: r["t"])
     total_boots = sum(circuits.bootstraps(r["gates"]) for r in reqs)
     result = {}
-    for form in ("split_fp32",):
+    for form in args.serve_forms.split(","):
         srv = pkg.Server(eng, pool_slots=131072, max_batch=4096, form=form)
         t0 = time.perf_counter()
         nxt = 0
@@ -527,15 +531,17 @@ def workload_serve(args, world, rank, local):
                                                   "p99": float(np.percentile(np.array(v) * 1000, 99)),
                                                   "n": len(v)} for k, v in lat.items() if v},
             "requests": len(reqs), "wrong_requests": wrong}
-    f = result["split_fp32"]
+    first = args.serve_forms.split(",")[0]
+    f = result[first]
     line = {"metric": "gate bootstraps/sec (serving)", "value": f["bootstraps_per_s"],
             "unit": "bootstraps/s", "n_gpus": 1, "steps": len(reqs), "warmup": 0,
             "ms_per_step": f["makespan_s"] * 1000 / len(reqs), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if first == "split_fp32" else "f64",
+            "data": "synthetic",
             "config": {"workload": "serving: %d clients x %d requests, Poisson arrivals %.1f req/s per "
                                    "client (seed 5); circuits uniform over 32-bit ripple-carry adder, "
-                                   "16-bit comparator, 8-bit multiplexer; one cloud key; split-FP32; "
-                                   "%d bootstraps in total" % (args.clients, args.requests, args.rate,
+                                   "16-bit comparator, 8-bit multiplexer; one cloud key; value = %s form; "
+                                   "%d bootstraps in total" % (args.clients, args.requests, args.rate, first,
                                                                total_boots)},
             "latency_ms": {"gate_p50": f["gate_latency_ms"]["p50"], "gate_p99": f["gate_latency_ms"]["p99"],
                            "request_p50": f["request_latency_ms"]["p50"],
@@ -571,9 +577,14 @@ def main():
     eng = pkg.Engine(P, device=local)
     eng.upload_bootstrapping_key(bk, forms=("fp64", "split_fp32"))
     eng.upload_keyswitch_key(ks)
+    batch = args.batch
+    tuned = None
     if args.groups:
         eng.set_groups_per_cta(args.form, args.groups)
-    batch = args.batch
+    elif not args.no_tune:
+        # project autotuner: time every launch shape on this batch size
+        shape, br_ms = eng.autotune(args.form, batch)
+        tuned = {"shape": shape, "blind_rotate_ms": br_ms}
     a, b, gates, ca, cb = make_inputs(pkg, P, lwe, batch)
     dev = torch.device("cuda", local)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
@@ -589,8 +600,15 @@ def main():
     d_out = torch.empty_like(d_ca)
     torch.cuda.synchronize()
 
+    # the whole gate pipeline of the batch as one CUDA graph (its creation
+    # runs the batch once); the FP64 side figures run eagerly
+    graph = None if args.no_graph else eng.graph_gates(d_g, d_out, d_ca, d_cb, batch, args.form)
+
     def step(form):
-        eng.bootsGates(d_g, d_out, d_ca, d_cb, batch, form, stream=sp)
+        if graph is not None and form == args.form:
+            graph.launch(stream=sp)
+        else:
+            eng.bootsGates(d_g, d_out, d_ca, d_cb, batch, form, stream=sp)
 
     # warm-up (also sizes the engine's scratch)
     for _ in range(args.warmup):
@@ -725,16 +743,18 @@ def main():
                                    "l=3, Bgbit=7, t=8, basebit=2), one cloud key (seed 0)" % batch,
                        "batch": batch, "form": args.form, "split_bits": eng.params.split_bits,
                        "groups_per_cta": eng.get_groups_per_cta(args.form),
+                       "autotune": tuned, "cuda_graph": graph is not None,
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": "replicas"},
             "latency_ms": {"p50": p50, "p99": p99,
                            "note": "per-gate latency = completion time of its batch"},
             "decrypt_ok": ok,
             "e2e": {"value": e2e_value, "unit": "bootstraps/s",
                     "h2d_bytes_per_step": 2 * lwe_bytes + batch * 4, "d2h_bytes_per_step": lwe_bytes},
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": (graph.kernels if graph is not None else 3) * args.steps,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": None,
-                         "kernel": "k_external_product<float,2,BlindRotate> (blind rotation + extraction)",
+                         "kernel": " + ".join(blind_rotate_kernels(args.form, eng.get_groups_per_cta(args.form),
+                                                                   batch)) + " (blind rotation + extraction)",
                          "kernel_ms": k_ms,
                          "peak_source": "nominal FP32 pipe: 152 SMs x 128 lanes x 2 x max SM clock "
                                         "(no measured FP32 peak in MEASURED_PEAKS.json)"},
@@ -744,9 +764,33 @@ def main():
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
+    if graph is not None:
+        graph.close()
     eng.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def blind_rotate_kernels(form, shape, batch, l=3):
+    """Names of the blind-rotation kernels a launch of `batch` runs with
+    launch shape `shape` (the engine's dispatch rules)."""
+    if form == "fp64":
+        return (["k_external_product<double,1,BlindRotate,3,%d>" % l] if shape == 3
+                else ["k_blind_rotate_ring<double,1,4,%d,4,inline>" % l])
+    ring = "k_blind_rotate_ring<float,2,%d,%d,4,%s>"
+    pair = "k_blind_rotate_pair<float,2,%d,%d,4>"
+    if shape == 0:
+        wave = 6 * SMS
+        full, rest = (batch // wave) * wave, batch - (batch // wave) * wave
+        if rest == 0 or rest > 3 * SMS:
+            return [ring % (6, l, "inline")]
+        names = [ring % (6, l, "inline") + " x %d" % full] if full else []
+        return names + [pair % ((rest + SMS - 1) // SMS, l) + " x %d" % rest]
+    if shape in (11, 12, 13):
+        return [pair % (shape - 10, l)]
+    if shape in (1, 2, 4):
+        return ["k_external_product<float,2,BlindRotate,%d,%d>" % (shape, l)]
+    return [ring % (shape, l, "producer-warp" if shape == 5 else "inline")]
 
 
 if __name__ == "__main__":

@@ -121,6 +121,35 @@ SIGNATURES = {
     "tfhe_gpu_server_poll": (ctypes.c_int, [VP, ctypes.c_int64, I32P, I32P,
                                              ctypes.POINTER(ctypes.c_double)]),
     "tfhe_gpu_server_stats": (ctypes.c_int, [VP, F64P, F64P, F64P, ctypes.POINTER(ctypes.c_int64)]),
+    "tfhe_gpu_upload_cloud_key": (ctypes.c_int, [VP, I32P, I32P, ctypes.c_uint32]),
+    "tfhe_gpu_bootsMUX_host": (ctypes.c_int, [VP, I32P, I32P, I32P, I32P, ctypes.c_int32, ctypes.c_int]),
+    "tfhe_gpu_upload_cloud_key_file": (ctypes.c_int, [VP, ctypes.c_char_p, ctypes.c_uint32]),
+    "tfhe_keyfile_bk_words": (ctypes.c_int64, [ctypes.c_void_p]),
+    "tfhe_keyfile_ks_words": (ctypes.c_int64, [ctypes.c_void_p]),
+    "tfhe_keyfile_peek": (ctypes.c_int, [VP, I32P, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    "tfhe_keyfile_write_params": (ctypes.c_int, [VP, ctypes.c_void_p]),
+    "tfhe_keyfile_write_cloud_key": (ctypes.c_int, [VP, ctypes.c_void_p, I32P, I32P]),
+    "tfhe_keyfile_write_secret_key": (ctypes.c_int, [VP, ctypes.c_void_p, I32P, I32P, I32P, I32P]),
+    "tfhe_keyfile_write_ciphertexts": (ctypes.c_int, [VP, ctypes.c_void_p, I32P, F64P, ctypes.c_int64]),
+    "tfhe_keyfile_read_params": (ctypes.c_int, [VP, ctypes.c_void_p]),
+    "tfhe_keyfile_read_cloud_key": (ctypes.c_int, [VP, ctypes.c_void_p, I32P, I32P]),
+    "tfhe_keyfile_read_secret_key": (ctypes.c_int, [VP, ctypes.c_void_p, I32P, I32P, I32P, I32P]),
+    "tfhe_keyfile_read_ciphertexts": (ctypes.c_int, [VP, ctypes.c_void_p, I32P, F64P,
+                                                     ctypes.POINTER(ctypes.c_int64)]),
+    "tfhe_keyfile_save_cloud_key": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, I32P, I32P]),
+    "tfhe_keyfile_load_cloud_key": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, I32P, I32P]),
+    "tfhe_gpu_graph_gates_create": (ctypes.c_int, [VP, VP, ctypes.c_int32, VP, VP, VP, ctypes.c_int32,
+                                                   ctypes.c_int, ctypes.POINTER(VP)]),
+    "tfhe_gpu_graph_launch": (ctypes.c_int, [VP, VP]),
+    "tfhe_gpu_graph_kernel_count": (ctypes.c_int32, [VP]),
+    "tfhe_gpu_graph_destroy": (None, [VP]),
+    "tfhe_gpu_autotune": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int32, I32P,
+                                         ctypes.POINTER(ctypes.c_float)]),
+    "tfhe_gpu_bootstrap_tv": (ctypes.c_int, [VP, VP, VP, VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int,
+                                             ctypes.c_int32, VP]),
+    "tfhe_client_encrypt_phases": (ctypes.c_int, [ctypes.c_void_p, I32P, ctypes.c_int32, I32P, I32P]),
+    "tfhe_client_test_vector": (ctypes.c_int, [ctypes.c_int32, I32P, ctypes.c_int32, I32P]),
+    "tfhe_gpu_gate_keyset": (ctypes.c_int, [VP, I32P, I32P, I32P, I32P, ctypes.c_uint32]),
     "tfhe_client_set_seed": (None, [U32P, ctypes.c_int32]),
     "tfhe_client_gate_keyset": (ctypes.c_int, [ctypes.c_void_p, I32P, I32P, I32P, I32P]),
     "tfhe_client_encrypt_bits": (ctypes.c_int, [ctypes.c_void_p, I32P, ctypes.c_int32, I32P, I32P]),
@@ -195,6 +224,32 @@ def encrypt_bits(P, bits, lwe_key):
     return out
 
 
+def encrypt_phases(P, mu, lwe_key):
+    """Encrypt Torus32 messages (one per sample)."""
+    mu = _np(mu, np.int32)
+    out = np.zeros((len(mu), P.n + 1), np.int32)
+    st = lib().tfhe_client_encrypt_phases(ctypes.byref(P), mu.ctypes.data_as(I32P), len(mu),
+                                          _np(lwe_key, np.int32).ctypes.data_as(I32P),
+                                          out.ctypes.data_as(I32P))
+    if st:
+        raise TfheError(st, "encrypt_phases")
+    return out
+
+
+def test_vector(N, table):
+    """Test vector (N int32) of a lookup table on len(table) padded messages."""
+    table = _np(table, np.int32)
+    tv = np.zeros(N, np.int32)
+    st = lib().tfhe_client_test_vector(N, table.ctypes.data_as(I32P), len(table), tv.ctypes.data_as(I32P))
+    if st:
+        raise TfheError(st, "test_vector")
+    return tv
+
+
+def mod_switch_to_torus32(mu, msize):
+    return lib().tfhe_client_mod_switch_to_torus32(int(mu), int(msize))
+
+
 def decrypt_bits(P, samples, lwe_key):
     s = _np(samples, np.int32).reshape(-1, P.n + 1)
     out = np.zeros(len(s), np.int32)
@@ -216,7 +271,169 @@ def phases(samples, key):
     return out
 
 
+# ---- key and ciphertext files (include/tfhe_keyfile.h) -----------------------
+
+KEYFILE_PARAMS, KEYFILE_CLOUD_KEY, KEYFILE_SECRET_KEY, KEYFILE_CIPHERTEXTS = 1, 2, 3, 4
+
+
+class _CFile:
+    """A C stdio stream on `path` for the FILE*-taking entry points."""
+    _libc = None
+
+    def __init__(self, path, mode):
+        if _CFile._libc is None:
+            libc = ctypes.CDLL(None)
+            libc.fopen.restype = VP
+            libc.fopen.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+            libc.fclose.restype = ctypes.c_int
+            libc.fclose.argtypes = [VP]
+            _CFile._libc = libc
+        self.f = _CFile._libc.fopen(os.fsencode(path), mode.encode())
+        if not self.f:
+            raise OSError("cannot open %s" % path)
+
+    def __enter__(self):
+        return self.f
+
+    def __exit__(self, *exc):
+        if _CFile._libc.fclose(self.f) != 0 and exc[0] is None:
+            raise OSError("close failed")
+
+
+def _kf(st, what):
+    if st:
+        raise TfheError(st, what)
+
+
+def keyfile_records(path):
+    """[(kind, params)] of every record in a file, in order (headers only)."""
+    out = []
+    with _CFile(path, "rb") as f:
+        L = lib()
+        while True:
+            kind = ctypes.c_int32()
+            P = Params()
+            if L.tfhe_keyfile_peek(f, ctypes.byref(kind), ctypes.byref(P), None):
+                break
+            out.append((kind.value, P))
+            # consume the record by reading it (checks the checksum too)
+            if kind.value == KEYFILE_PARAMS:
+                _kf(L.tfhe_keyfile_read_params(f, None), "read_params")
+            elif kind.value == KEYFILE_CLOUD_KEY:
+                _kf(L.tfhe_keyfile_read_cloud_key(f, None, None, None), "read_cloud_key")
+            elif kind.value == KEYFILE_SECRET_KEY:
+                _kf(L.tfhe_keyfile_read_secret_key(f, None, None, None, None, None), "read_secret_key")
+            elif kind.value == KEYFILE_CIPHERTEXTS:
+                c = ctypes.c_int64(0)
+                _kf(L.tfhe_keyfile_read_ciphertexts(f, None, None, None, ctypes.byref(c)),
+                    "read_ciphertexts")
+            else:
+                break
+    return out
+
+
+def save_cloud_key(path, P, bk, ks):
+    _kf(lib().tfhe_keyfile_save_cloud_key(os.fsencode(path), ctypes.byref(P),
+                                          _np(bk, np.int32).ctypes.data_as(I32P),
+                                          _np(ks, np.int32).ctypes.data_as(I32P)), "save_cloud_key")
+
+
+def load_cloud_key(path):
+    """(params, bk, ks) of a cloud-key file."""
+    with _CFile(path, "rb") as f:
+        kind = ctypes.c_int32()
+        P = Params()
+        _kf(lib().tfhe_keyfile_peek(f, ctypes.byref(kind), ctypes.byref(P), None), "peek")
+    bk = np.zeros(lib().tfhe_keyfile_bk_words(ctypes.byref(P)), np.int32)
+    ks = np.zeros(lib().tfhe_keyfile_ks_words(ctypes.byref(P)), np.int32)
+    _kf(lib().tfhe_keyfile_load_cloud_key(os.fsencode(path), ctypes.byref(P), bk.ctypes.data_as(I32P),
+                                          ks.ctypes.data_as(I32P)), "load_cloud_key")
+    return P, bk, ks
+
+
+def save_secret_key(path, P, lwe_key, tlwe_key, bk, ks):
+    with _CFile(path, "wb") as f:
+        _kf(lib().tfhe_keyfile_write_secret_key(
+            f, ctypes.byref(P), _np(lwe_key, np.int32).ctypes.data_as(I32P),
+            _np(tlwe_key, np.int32).ctypes.data_as(I32P), _np(bk, np.int32).ctypes.data_as(I32P),
+            _np(ks, np.int32).ctypes.data_as(I32P)), "write_secret_key")
+
+
+def load_secret_key(path):
+    """(params, lwe_key, tlwe_key, bk, ks) of a secret-key file."""
+    with _CFile(path, "rb") as f:
+        kind = ctypes.c_int32()
+        P = Params()
+        _kf(lib().tfhe_keyfile_peek(f, ctypes.byref(kind), ctypes.byref(P), None), "peek")
+        lwe = np.zeros(P.n, np.int32)
+        tlwe = np.zeros(P.k * P.N, np.int32)
+        bk = np.zeros(lib().tfhe_keyfile_bk_words(ctypes.byref(P)), np.int32)
+        ks = np.zeros(lib().tfhe_keyfile_ks_words(ctypes.byref(P)), np.int32)
+        _kf(lib().tfhe_keyfile_read_secret_key(f, ctypes.byref(P), lwe.ctypes.data_as(I32P),
+                                               tlwe.ctypes.data_as(I32P), bk.ctypes.data_as(I32P),
+                                               ks.ctypes.data_as(I32P)), "read_secret_key")
+    return P, lwe, tlwe, bk, ks
+
+
+def save_ciphertexts(path, P, samples, append=False):
+    s = _np(samples, np.int32).reshape(-1, P.n + 1)
+    with _CFile(path, "ab" if append else "wb") as f:
+        _kf(lib().tfhe_keyfile_write_ciphertexts(f, ctypes.byref(P), s.ctypes.data_as(I32P), None,
+                                                 len(s)), "write_ciphertexts")
+
+
+def load_ciphertexts(path):
+    """All ciphertext records of a file, concatenated: int32[count][n+1]."""
+    out = []
+    with _CFile(path, "rb") as f:
+        L = lib()
+        while True:
+            kind = ctypes.c_int32()
+            P = Params()
+            items = ctypes.c_int64(0)
+            if L.tfhe_keyfile_peek(f, ctypes.byref(kind), ctypes.byref(P), ctypes.byref(items)):
+                break
+            buf = np.zeros((items.value, P.n + 1), np.int32)
+            _kf(L.tfhe_keyfile_read_ciphertexts(f, None, buf.ctypes.data_as(I32P), None,
+                                                ctypes.byref(items)), "read_ciphertexts")
+            out.append(buf)
+    if not out:
+        raise TfheError(1, "no ciphertext records in %s" % path)
+    return np.concatenate(out)
+
+
 # ---- engine ------------------------------------------------------------------
+
+class Graph:
+    """tfhe_gpu_graph: a captured gate batch, replayed by launch()."""
+
+    def __init__(self, eng, gates, out, ca, cb, count, form, uniform_gate):
+        self.eng = eng
+        self.lib = eng.lib
+        h = VP()
+        eng._check(self.lib.tfhe_gpu_graph_gates_create(eng.ctx, _ptr(gates), int(uniform_gate), _ptr(out),
+                                                        _ptr(ca), _ptr(cb), int(count), eng._form(form),
+                                                        ctypes.byref(h)), "graph_gates_create")
+        self.h = h
+
+    @property
+    def kernels(self):
+        return self.lib.tfhe_gpu_graph_kernel_count(self.h)
+
+    def launch(self, stream=None):
+        self.eng._check(self.lib.tfhe_gpu_graph_launch(self.h, stream), "graph_launch")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tfhe_gpu_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 class Engine:
     """One engine context on one device (tfhe_gpu_ctx)."""
@@ -289,6 +506,61 @@ class Engine:
         self._check(self.lib.tfhe_gpu_upload_bootstrapping_key_fft(
             self.ctx, bk_fft.ctypes.data_as(F64P), mask), "upload_bootstrapping_key_fft")
 
+    def gate_keyset(self, seed, forms=("fp64", "split_fp32"), want_bk=True):
+        """Seed the client generator and generate (lwe, tlwe, ks, bk) with the
+        bootstrapping key's arithmetic on the GPU; the keys are uploaded."""
+        P = self.params
+        set_seed(seed)
+        lwe = np.zeros(P.n, np.int32)
+        tlwe = np.zeros(P.k * P.N, np.int32)
+        ks = np.zeros(P.ks_words(), np.int32)
+        bk = np.zeros(P.n * P.tgsw_words(), np.int32) if want_bk else None
+        mask = 0
+        for f in forms:
+            mask |= 1 << FORMS[f]
+        self._check(self.lib.tfhe_gpu_gate_keyset(self.ctx, lwe.ctypes.data_as(I32P), tlwe.ctypes.data_as(I32P),
+                                                  ks.ctypes.data_as(I32P),
+                                                  bk.ctypes.data_as(I32P) if want_bk else None, mask),
+                    "gate_keyset")
+        return lwe, tlwe, ks, bk
+
+    def autotune(self, form, count):
+        """Time the launch shapes on `count` ciphertexts; keeps and returns
+        (shape, ms) of the fastest."""
+        shape = ctypes.c_int32()
+        ms = ctypes.c_float()
+        self._check(self.lib.tfhe_gpu_autotune(self.ctx, self._form(form), int(count), ctypes.byref(shape),
+                                               ctypes.byref(ms)), "autotune")
+        return shape.value, ms.value
+
+    def graph_gates(self, gates, out, ca, cb, count, form="split_fp32", uniform_gate=0):
+        """A CUDA graph of the gate pipeline over fixed device buffers."""
+        return Graph(self, gates, out, ca, cb, count, form, uniform_gate)
+
+    def upload_cloud_key(self, bk, ks, forms=("fp64", "split_fp32")):
+        mask = 0
+        for f in forms:
+            mask |= 1 << FORMS[f]
+        self._check(self.lib.tfhe_gpu_upload_cloud_key(self.ctx, _np(bk, np.int32).ctypes.data_as(I32P),
+                                                       _np(ks, np.int32).ctypes.data_as(I32P), mask),
+                    "upload_cloud_key")
+
+    def upload_cloud_key_file(self, path, forms=("fp64", "split_fp32")):
+        mask = 0
+        for f in forms:
+            mask |= 1 << FORMS[f]
+        self._check(self.lib.tfhe_gpu_upload_cloud_key_file(self.ctx, os.fsencode(path), mask),
+                    "upload_cloud_key_file")
+
+    def bootsMUX_host(self, a, b, c, form="split_fp32"):
+        a, b, c = (_np(x, np.int32).reshape(-1, self.params.n + 1) for x in (a, b, c))
+        out = np.zeros_like(a)
+        self._check(self.lib.tfhe_gpu_bootsMUX_host(self.ctx, out.ctypes.data_as(I32P),
+                                                    a.ctypes.data_as(I32P), b.ctypes.data_as(I32P),
+                                                    c.ctypes.data_as(I32P), len(a), self._form(form)),
+                    "bootsMUX_host")
+        return out
+
     def upload_keyswitch_key(self, ks):
         ks = _np(ks, np.int32)
         self._check(self.lib.tfhe_gpu_upload_keyswitch_key(self.ctx, ks.ctypes.data_as(I32P)),
@@ -359,6 +631,12 @@ class Engine:
         g = GATES[gate] if isinstance(gate, str) else int(gate)
         self._check(self.lib.tfhe_gpu_bootsGate(self.ctx, g, _ptr(out), _ptr(ca), _ptr(cb), count,
                                                 self._form(form), stream), "bootsGate")
+
+    def bootstrap_tv(self, out, x, tv, count, form, tv_stride=0, keyswitch=True, stream=None):
+        """Programmable bootstrap of `count` samples with test vector(s) tv."""
+        self._check(self.lib.tfhe_gpu_bootstrap_tv(self.ctx, _ptr(out), _ptr(x), _ptr(tv), int(tv_stride),
+                                                   int(count), self._form(form), 1 if keyswitch else 0,
+                                                   stream), "bootstrap_tv")
 
     def bootsGates(self, gates, out, ca, cb, count, form, stream=None):
         self._check(self.lib.tfhe_gpu_bootsGates(self.ctx, _ptr(gates), _ptr(out), _ptr(ca), _ptr(cb),

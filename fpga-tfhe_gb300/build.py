@@ -41,7 +41,8 @@ def _sources():
 
 def _headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    hs += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+    for d in (INCLUDE, os.path.join(INCLUDE, "tfhe")):
+        hs += [os.path.join(d, f) for f in os.listdir(d) if f.endswith(".h")]
     return hs
 
 

@@ -68,6 +68,18 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     return true;
 }
 
+// The same with a CTA-wide abort flag: once any wait of the CTA has given up
+// (and set *abort), the others return false at once instead of waiting out
+// their own limit, so a failed kernel ends within about one limit.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  const volatile int* abort) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (*abort || global_ns() - t0 > kWaitLimitNs) return false;
+    }
+    return true;
+}
 // Bulk copy global -> this CTA's shared memory; completion is counted in
 // bytes on `bar`.  dst, src 16-byte aligned; bytes a multiple of 16.
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes,

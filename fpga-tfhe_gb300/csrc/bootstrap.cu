@@ -34,12 +34,15 @@ namespace {
 constexpr int kN = 1024;
 constexpr int kHalf = 512;
 // Table layout (complex entries): W^(tq) as [q][t] (512), W^(8jq) as [q][j]
-// (64), then psi^x (512).
+// (64), psi^t W^(tq) as [q][t] (512), then psi^x (512).  The blind-rotation
+// and external-product kernels keep only the "hot" part [kTabB, kTabB +
+// kHotSize) in shared memory: W^(8jq) at 0, psi^t W^(tq) at 64.
 constexpr int kTabA = 0;
 constexpr int kTabB = 512;
-constexpr int kTabPsi = 576;
-constexpr int kTabSize = 1088;
-constexpr int kSmCount = 152;  // GB300
+constexpr int kTabT = 576;
+constexpr int kTabPsi = 1088;
+constexpr int kTabSize = 1600;
+constexpr int kHotSize = 576;
 
 // ----------------------------------------------------------------------
 // helpers
@@ -70,6 +73,43 @@ __device__ __forceinline__ int32_t rot_coef(const int32_t* p, int x, int a) {
     return s < kN ? v : (int32_t)(0u - (uint32_t)v);
 }
 
+// Coefficient i of X^{2N - barb} tv: the rotated test vector the blind
+// rotation starts from.  tv = nullptr is the constant mu of the gate
+// bootstrap (tfhe_bootstrap_woKS_FFT.cpp:63-66, mulByXaiOrCopy.cpp:25-41),
+// else the polynomial of item c (programmable bootstrap).
+__device__ __forceinline__ int32_t test_vector_coef(const EpArgs& a, int c, int barb, int i) {
+    if (!a.tv) return (((i + barb) & (2 * kN - 1)) < kN) ? a.mu : -a.mu;
+    return rot_coef(a.tv + (size_t)c * a.tv_stride, i, (2 * kN - barb) & (2 * kN - 1));
+}
+
+// Rounding the inverse transform's FP32 output to Torus32 without a float ->
+// int64 conversion (on this part that conversion issues to the narrow FP64
+// pipe): FP32 adds and FMAs plus integer adds.  M = 1.5 * 2^23: for |y| <
+// 2^22 the sum y + M rounds y to the nearest integer, whose two's complement
+// is then the low bits of the sum's encoding.
+constexpr float kRoundMagic = 12582912.0f;
+constexpr int32_t kRoundMagicBits = 0x4B400000;
+
+// round(v / 512) mod 2^32 for |v / 512| < 2^22 (the high key part's product:
+// about 2^18 typical, the exactness limit of FP32 is 2^24).
+__device__ __forceinline__ uint32_t round_small_u32(float v) {
+    return (uint32_t)(__float_as_int(fmaf(v, 0x1p-9f, kRoundMagic)) - kRoundMagicBits);
+}
+
+// round(v / 512) mod 2^32 for any |v / 512| < 2^53 (the low key part's
+// product, up to about 2^36): remove the multiple of 2^32, then split the
+// remainder (|a| <= 2^31) into 2^16 a1 + a2 and round both pieces with the
+// magic constant.  Every step is exact in FP32.
+__device__ __forceinline__ uint32_t round_wrap_u32(float v) {
+    const float q = fmaf(v, 0x1p-41f, kRoundMagic) - kRoundMagic;  // rint(v / 2^41)
+    const float a = fmaf(-q, 0x1p41f, v);                             // exact, |a| <= 2^40
+    const float u1 = fmaf(a, 0x1p-25f, kRoundMagic);                  // rint(a / 2^25) in the low bits
+    const float a2 = fmaf(-(u1 - kRoundMagic), 0x1p25f, a);           // exact, |a2| <= 2^24
+    const int32_t i1 = __float_as_int(u1) - kRoundMagicBits;
+    const int32_t i2 = __float_as_int(fmaf(a2, 0x1p-9f, kRoundMagic)) - kRoundMagicBits;
+    return ((uint32_t)i1 << 16) + (uint32_t)i2;
+}
+
 template <typename R>
 __device__ __forceinline__ int64_t to_int(R v);
 template <>
@@ -90,7 +130,7 @@ __device__ __forceinline__ int64_t to_int<float>(float v) {
 // ----------------------------------------------------------------------
 template <typename R, int NB>
 struct SmemPlan {
-    static constexpr size_t tables = kTabSize * sizeof(cpx<R>);
+    static constexpr size_t tables = kHotSize * sizeof(cpx<R>);
     static constexpr size_t acc = 2 * kN * sizeof(int32_t);
     static constexpr size_t scratch = NB * 2 * kScratchStride * sizeof(cpx<R>);
     static constexpr size_t group = acc + scratch;
@@ -114,6 +154,18 @@ __device__ __forceinline__ FftTwiddles<R> twiddles_at(const cpx<R>* tables) {
     return {tables + kTabA, tables + kTabB};
 }
 
+// the hot tables (twist-folded pass-A twiddles, pass-B twiddles)
+template <typename R>
+__device__ __forceinline__ void load_hot_tables(cpx<R>* dst, const Tables& T) {
+    const cpx<R>* src = table_ptr<R>(T) + kTabB;
+    for (int i = threadIdx.x; i < kHotSize; i += blockDim.x) dst[i] = src[i];
+}
+
+template <typename R>
+__device__ __forceinline__ FftTwiddles<R> hot_twiddles(const cpx<R>* hot) {
+    return {hot + (kTabT - kTabB), hot};
+}
+
 // ----------------------------------------------------------------------
 // the fused step: out = EP(ROT ? (X^a - 1) acc : acc);
 //                 acc = (ROT ? acc : 0) + out
@@ -128,8 +180,7 @@ __device__ __forceinline__ FftTwiddles<R> twiddles_at(const cpx<R>* tables) {
 // ----------------------------------------------------------------------
 template <typename R, int PARTS, int NB>
 struct StepCtx {
-    FftTwiddles<R> tw;  // smem W_512 powers, per pass
-    const cpx<R>* psi;  // smem psi^x
+    FftTwiddles<R> tw;  // smem twiddles: a = psi^t W^(tq) (twist folded), b = W^(8jq)
     FftScratch<R> s[NB];
     int32_t* acc;       // smem 2 x N
     int t, bar_id;
@@ -223,17 +274,16 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
             cpx<R> v[FB][8];
 #pragma unroll
             for (int r = 0; r < 8; ++r) {
-                const cpx<R> ps = S.psi[t + 64 * r];
 #pragma unroll
                 for (int b = 0; b < FB; ++b) {
                     const int decal = 32 - (lev0 + b + 1) * S.Bgbit;
                     const int d0 = (int)((r0[r] >> decal) & mask) - halfBg;
                     const int d1 = (int)((r1[r] >> decal) & mask) - halfBg;
-                    v[b][r] = cmul(cpx<R>{(R)d0, (R)d1}, ps);
+                    v[b][r] = cpx<R>{(R)d0, (R)d1};
                 }
             }
-            fft512_forward_multi<FB>(v, *reinterpret_cast<const FftScratch<R>(*)[FB]>(S.s), S.tw, t,
-                                     S.bar_id);
+            fft512_forward_tw_multi<FB>(v, *reinterpret_cast<const FftScratch<R>(*)[FB]>(S.s), S.tw, t,
+                                        S.bar_id);
 #pragma unroll
             for (int b = 0; b < FB; ++b) {
                 const int p = jp * L + lev0 + b;
@@ -255,17 +305,27 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
             for (int b = 0; b < IB; ++b)
 #pragma unroll
                 for (int q = 0; q < 8; ++q) v[b][q] = out[j][pt0 + b][q];
-            fft512_inverse_multi<IB>(v, *reinterpret_cast<const FftScratch<R>(*)[IB]>(S.s), S.tw, t,
-                                     S.bar_id);
+            fft512_inverse_tw_multi<IB>(v, *reinterpret_cast<const FftScratch<R>(*)[IB]>(S.s), S.tw, t,
+                                        S.bar_id);
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                const cpx<R> ps = S.psi[t + 64 * q];
 #pragma unroll
                 for (int b = 0; b < IB; ++b) {
                     const int pt = pt0 + b;
-                    const cpx<R> z = cmulc(v[b][q], ps);
-                    const uint32_t a0 = (uint32_t)(uint64_t)to_int<R>(z.x * inv);
-                    const uint32_t a1 = (uint32_t)(uint64_t)to_int<R>(z.y * inv);
+                    const cpx<R> z = v[b][q];
+                    uint32_t a0, a1;
+                    if constexpr (sizeof(R) == 4) {
+                        if (PARTS == 2 && pt == 0) {
+                            a0 = round_small_u32(z.x);
+                            a1 = round_small_u32(z.y);
+                        } else {
+                            a0 = round_wrap_u32(z.x);
+                            a1 = round_wrap_u32(z.y);
+                        }
+                    } else {
+                        a0 = (uint32_t)(uint64_t)to_int<R>(z.x * inv);
+                        a1 = (uint32_t)(uint64_t)to_int<R>(z.y * inv);
+                    }
                     if (PARTS == 1) {
                         c0[q] = a0;
                         c1[q] = a1;
@@ -307,7 +367,7 @@ __global__ void __launch_bounds__(64 * GROUPS, 1) k_external_product(KParams kp,
     using Plan = SmemPlan<R, NB>;
     extern __shared__ __align__(16) char smem[];
     cpx<R>* tables = reinterpret_cast<cpx<R>*>(smem);
-    load_tables<R>(tables, T);
+    load_hot_tables<R>(tables, T);
     __syncthreads();
 
     const int g = threadIdx.x >> 6;
@@ -317,8 +377,7 @@ __global__ void __launch_bounds__(64 * GROUPS, 1) k_external_product(KParams kp,
 
     char* gbase = smem + Plan::tables + (size_t)g * Plan::group;
     Ctx S;
-    S.tw = twiddles_at<R>(tables);
-    S.psi = tables + kTabPsi;
+    S.tw = hot_twiddles<R>(tables);
     S.acc = reinterpret_cast<int32_t*>(gbase);
 #pragma unroll
     for (int b = 0; b < NB; ++b)
@@ -344,7 +403,7 @@ __global__ void __launch_bounds__(64 * GROUPS, 1) k_external_product(KParams kp,
             const int barb = mod_switch_2n(xs[n]);
             for (int i = t; i < kN; i += 64) {
                 S.acc[i] = 0;
-                S.acc[kN + i] = (((i + barb) & (2 * kN - 1)) < kN) ? a.mu : -a.mu;
+                S.acc[kN + i] = test_vector_coef(a, c, barb, i);
             }
         }
         group_sync(S.bar_id);
@@ -414,6 +473,7 @@ struct RingKeys {
     uint64_t* empty;
     uint32_t row0;
     int32_t* err;
+    volatile int* abort;   // CTA-wide: set by the first wait that gives up
     // In-line producer (one thread of the CTA when there is no producer
     // warp): before taking row r it issues rows up to r + S - 1, waiting only
     // for rows it needs itself (<= r) and skipping ahead rows whose slot is
@@ -423,25 +483,48 @@ struct RingKeys {
     uint32_t total;        // rows to stream
     uint32_t next_issue;   // first row not issued yet
 
+    __device__ __forceinline__ void give_up() {
+        *abort = 1;
+        atomicExch(err, 3);
+    }
+    __device__ __forceinline__ void issue_one() {
+        const uint32_t slot = next_issue % S;
+        mbar_arrive_expect_tx(&full[slot], (uint32_t)kRowBytes);
+        bulk_copy_g2s(reinterpret_cast<char*>(ring) + slot * kRowBytes,
+                      src + (size_t)next_issue * kRowBytes, (uint32_t)kRowBytes, &full[slot]);
+        ++next_issue;
+    }
     __device__ __forceinline__ void issue_upto(uint32_t r) {
         while (next_issue < total && next_issue < r + S) {
             const uint32_t slot = next_issue % S;
             if (next_issue >= S) {
                 const uint32_t parity = ((next_issue / S) - 1) & 1;
                 if (next_issue <= r) {
-                    if (!mbar_wait_bounded(&empty[slot], parity)) {
-                        atomicExch(err, 3);
-                        next_issue = total;  // stop streaming; consumers time out and finish
+                    if (!mbar_wait_bounded(&empty[slot], parity, abort)) {
+                        give_up();
+                        next_issue = total;  // stop streaming; consumers give up and finish
                         return;
                     }
                 } else if (!mbar_try_wait(&empty[slot], parity)) {
                     return;
                 }
             }
-            mbar_arrive_expect_tx(&full[slot], (uint32_t)kRowBytes);
-            bulk_copy_g2s(reinterpret_cast<char*>(ring) + slot * kRowBytes,
-                          src + (size_t)next_issue * kRowBytes, (uint32_t)kRowBytes, &full[slot]);
-            ++next_issue;
+            issue_one();
+        }
+    }
+    // Issue every row up to `last` (inclusive), waiting for their slots: used
+    // before the producer blocks on another group, for rows that group needs.
+    // Deadlock-free as long as the rows whose slots are reused (<= last - S)
+    // are released by consumers that need only rows already issued.
+    __device__ __forceinline__ void issue_through(uint32_t last) {
+        while (next_issue < total && next_issue <= last) {
+            if (next_issue >= S &&
+                !mbar_wait_bounded(&empty[next_issue % S], ((next_issue / S) - 1) & 1, abort)) {
+                give_up();
+                next_issue = total;
+                return;
+            }
+            issue_one();
         }
     }
     // wait until every issued copy has landed (end of kernel)
@@ -454,7 +537,7 @@ struct RingKeys {
         const uint32_t r = row0 + (uint32_t)p;
         if (producer) issue_upto(r);
         const uint32_t slot = r % S;
-        if (!mbar_wait_bounded(&full[slot], (r / S) & 1)) atomicExch(err, 3);
+        if (!mbar_wait_bounded(&full[slot], (r / S) & 1, abort)) give_up();
         return ring + slot * kRow;
     }
     __device__ __forceinline__ void release(int p) const { mbar_arrive(&empty[(row0 + (uint32_t)p) % S]); }
@@ -463,10 +546,11 @@ struct RingKeys {
 template <typename R, int PARTS, int GROUPS, int L, int S>
 struct RingPlan {
     static constexpr size_t kRowBytes = (size_t)2 * PARTS * kHalf * sizeof(cpx<R>);
-    static constexpr size_t tables = kTabSize * sizeof(cpx<R>);
+    static constexpr size_t tables = kHotSize * sizeof(cpx<R>);
     static constexpr size_t ring_off = (tables + 127) & ~(size_t)127;
     static constexpr size_t bar_off = ring_off + S * kRowBytes;
-    static constexpr size_t group_off = bar_off + 2 * S * sizeof(uint64_t);
+    static constexpr size_t flag_off = bar_off + 2 * S * sizeof(uint64_t);
+    static constexpr size_t group_off = (flag_off + sizeof(int) + 127) & ~(size_t)127;
     static constexpr size_t acc = 2 * kN * sizeof(int32_t);
     static constexpr size_t group = acc + 2 * kScratchStride * sizeof(cpx<R>);
     static constexpr size_t total = group_off + GROUPS * group;
@@ -482,21 +566,23 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
     cpx<R>* ring = reinterpret_cast<cpx<R>*>(smem + Plan::ring_off);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + Plan::bar_off);
     uint64_t* empty = full + S;
+    volatile int* abort = reinterpret_cast<volatile int*>(smem + Plan::flag_off);
     const int active = min(GROUPS, a.count - (int)blockIdx.x * GROUPS);
     if (threadIdx.x == 0) {
         for (int i = 0; i < S; ++i) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 64 * active);
         }
+        *abort = 0;
         fence_mbar_init();
     }
-    load_tables<R>(tables, T);
+    load_hot_tables<R>(tables, T);
     __syncthreads();
 
     const int warp = threadIdx.x >> 5;
     const int n = kp.n;
     const uint32_t total_rows = (uint32_t)n * kpl;
-    RingKeys<R, PARTS, S> keys{ring, full, empty, 0, a.err, false,
+    RingKeys<R, PARTS, S> keys{ring, full, empty, 0, a.err, abort, false,
                                reinterpret_cast<const char*>(a.gsw), total_rows, 0};
     if (!INLINE && warp == 2 * GROUPS) {
         // producer warp: one lane streams all n * 2l key rows in order
@@ -518,8 +604,7 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
 
     char* gbase = smem + Plan::group_off + (size_t)g * Plan::group;
     StepCtx<R, PARTS, 1> St;
-    St.tw = twiddles_at<R>(tables);
-    St.psi = tables + kTabPsi;
+    St.tw = hot_twiddles<R>(tables);
     St.acc = reinterpret_cast<int32_t*>(gbase);
     St.s[0] = scratch_at<R>(gbase + Plan::acc);
     St.t = t;
@@ -536,7 +621,7 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
         const int barb = mod_switch_2n(xs[n]);
         for (int i = t; i < kN; i += 64) {
             St.acc[i] = 0;
-            St.acc[kN + i] = (((i + barb) & (2 * kN - 1)) < kN) ? a.mu : -a.mu;
+            St.acc[kN + i] = test_vector_coef(a, c, barb, i);
         }
     }
     group_sync(St.bar_id);
@@ -567,6 +652,247 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
         for (int i = t; i < kN; i += 64)
             dst[i] = i == 0 ? St.acc[0] : (int32_t)(0u - (uint32_t)St.acc[kN - i]);
         if (t == 0) dst[kN] = St.acc[kN];
+    }
+}
+
+// ----------------------------------------------------------------------
+// Blind rotation with two 64-thread halves per ciphertext (low latency).
+//
+// Half h of a ciphertext decomposes and transforms input polynomial h (rows
+// h l .. h l + l - 1 of every key step), multiply-accumulates them into the
+// partial products of both output polynomials, hands the partial of output
+// 1 - h to the other half through shared memory, and transforms back only
+// output h.  Each half reads and writes only accumulator polynomial h, so the
+// halves meet once per step (the partial exchange).  Per step and half: l
+// forward and PARTS inverse transforms instead of 2l and 2 PARTS, so a
+// ciphertext takes about half the time; used when a batch has at most three
+// ciphertexts per SM to spread (the last partial wave of a large batch,
+// small batches, single gates).  Key rows come through the same shared ring
+// as k_blind_rotate_ring; each row is read by one half of every ciphertext.
+// ----------------------------------------------------------------------
+__device__ __forceinline__ void pair_sync(int bar_id) {
+    asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(2 * kFftThreads) : "memory");
+}
+
+// H is the half (a compile-time constant so that out[H] and out[1 - H] stay
+// in registers).
+template <typename R, int PARTS, int L, int H, typename Keys>
+__device__ __forceinline__ void ep_step_half(const StepCtx<R, PARTS, 1>& S, Keys& keys, int a,
+                                             cpx<R>* peer_inbox, int pair_bar) {
+    constexpr int h = H;
+    const int t = S.t;
+    const int halfBg = 1 << (S.Bgbit - 1);
+    const uint32_t mask = (1u << S.Bgbit) - 1;
+
+    cpx<R> out[2][PARTS][8];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int pt = 0; pt < PARTS; ++pt)
+#pragma unroll
+            for (int q = 0; q < 8; ++q) out[j][pt][q] = {(R)0, (R)0};
+
+    {
+        const int32_t* src = S.acc + h * kN;
+        uint32_t r0[8], r1[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int x0 = t + 64 * r;
+            r0[r] = (uint32_t)rot_coef(src, x0, a) - (uint32_t)src[x0] + S.offset;
+            r1[r] = (uint32_t)rot_coef(src, x0 + kHalf, a) - (uint32_t)src[x0 + kHalf] + S.offset;
+        }
+#pragma unroll
+        for (int lev = 0; lev < L; ++lev) {
+            cpx<R> v[8];
+            const int decal = 32 - (lev + 1) * S.Bgbit;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int d0 = (int)((r0[r] >> decal) & mask) - halfBg;
+                const int d1 = (int)((r1[r] >> decal) & mask) - halfBg;
+                v[r] = cpx<R>{(R)d0, (R)d1};
+            }
+            fft512_forward_tw(v, S.s[0], S.tw, t, S.bar_id);
+            const int p = h * L + lev;
+            mac_row<R, PARTS, Keys::kShared>(out, v, keys.acquire(p), t);
+            keys.release(p);
+        }
+    }
+    // every row of this step is issued before the producer waits on its pair
+    if (keys.producer) keys.issue_through(keys.row0 + 2 * L - 1);
+
+    // exchange: both halves' forward transforms are done, so their scratch
+    // buffers are free; write the partial of output 1 - h into the other
+    // half's scratch, then read this half's own
+    pair_sync(pair_bar);
+#pragma unroll
+    for (int pt = 0; pt < PARTS; ++pt)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) peer_inbox[pt * kScratchStride + q * 64 + t] = out[1 - h][pt][q];
+    pair_sync(pair_bar);
+    // the next step's first rows land during this step's inverse transforms
+    if (keys.producer) keys.issue_upto(keys.row0 + 2 * L - 1);
+    {
+        const cpx<R>* inbox = S.s[0].b0;
+#pragma unroll
+        for (int pt = 0; pt < PARTS; ++pt)
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                out[h][pt][q] = cadd(out[h][pt][q], inbox[pt * kScratchStride + q * 64 + t]);
+    }
+    group_sync(S.bar_id);  // the inbox is the transform's scratch
+
+    const R inv = (R)(1.0 / 512.0);
+    uint32_t c0[8], c1[8];
+#pragma unroll
+    for (int pt = 0; pt < PARTS; ++pt) {
+        cpx<R> v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = out[h][pt][q];
+        fft512_inverse_tw(v, S.s[0], S.tw, t, S.bar_id);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const cpx<R> z = v[q];
+            uint32_t a0, a1;
+            if constexpr (sizeof(R) == 4) {
+                if (PARTS == 2 && pt == 0) {
+                    a0 = round_small_u32(z.x);
+                    a1 = round_small_u32(z.y);
+                } else {
+                    a0 = round_wrap_u32(z.x);
+                    a1 = round_wrap_u32(z.y);
+                }
+            } else {
+                a0 = (uint32_t)(uint64_t)to_int<R>(z.x * inv);
+                a1 = (uint32_t)(uint64_t)to_int<R>(z.y * inv);
+            }
+            if (PARTS == 1) {
+                c0[q] = a0;
+                c1[q] = a1;
+            } else if (pt == 0) {
+                c0[q] = a0 << S.split;
+                c1[q] = a1 << S.split;
+            } else {
+                c0[q] += a0;
+                c1[q] += a1;
+            }
+        }
+    }
+    int32_t* dst = S.acc + h * kN;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int x0 = t + 64 * q;
+        dst[x0] = (int32_t)((uint32_t)dst[x0] + c0[q]);
+        dst[x0 + kHalf] = (int32_t)((uint32_t)dst[x0 + kHalf] + c1[q]);
+    }
+    group_sync(S.bar_id);
+}
+
+template <typename R, int PARTS, int PAIRS, int L, int S>
+struct PairPlan {
+    static constexpr size_t kRowBytes = (size_t)2 * PARTS * kHalf * sizeof(cpx<R>);
+    static constexpr size_t tables = kHotSize * sizeof(cpx<R>);
+    static constexpr size_t ring_off = (tables + 127) & ~(size_t)127;
+    static constexpr size_t bar_off = ring_off + S * kRowBytes;
+    static constexpr size_t flag_off = bar_off + 2 * S * sizeof(uint64_t);
+    static constexpr size_t pair_off = (flag_off + sizeof(int) + 127) & ~(size_t)127;
+    static constexpr size_t acc = 2 * kN * sizeof(int32_t);
+    static constexpr size_t half_scratch = 2 * kScratchStride * sizeof(cpx<R>);
+    static constexpr size_t pair = acc + 2 * half_scratch;
+    static constexpr size_t total = pair_off + PAIRS * pair;
+};
+
+template <typename R, int PARTS, int PAIRS, int L, int S>
+__global__ void __launch_bounds__(128 * PAIRS, 1) k_blind_rotate_pair(KParams kp, Tables T, EpArgs a) {
+    using Plan = PairPlan<R, PARTS, PAIRS, L, S>;
+    static_assert(1 + 2 * PAIRS + PAIRS <= 16, "named barriers");
+    static_assert(PARTS * kScratchStride >= PARTS * kHalf, "inbox fits the scratch");
+    constexpr int kpl = 2 * L;
+    extern __shared__ __align__(128) char smem[];
+    cpx<R>* tables = reinterpret_cast<cpx<R>*>(smem);
+    cpx<R>* ring = reinterpret_cast<cpx<R>*>(smem + Plan::ring_off);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + Plan::bar_off);
+    uint64_t* empty = full + S;
+    volatile int* abort = reinterpret_cast<volatile int*>(smem + Plan::flag_off);
+    const int active = min(PAIRS, a.count - (int)blockIdx.x * PAIRS);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < S; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 64 * active);  // one half of every ciphertext reads a row
+        }
+        *abort = 0;
+        fence_mbar_init();
+    }
+    load_hot_tables<R>(tables, T);
+    __syncthreads();
+
+    const int pr = threadIdx.x >> 7;
+    const int h = (threadIdx.x >> 6) & 1;
+    const int t = threadIdx.x & 63;
+    const int c = blockIdx.x * PAIRS + pr;
+    if (pr >= active) return;
+    const int n = kp.n;
+    RingKeys<R, PARTS, S> keys{ring, full, empty, 0, a.err, abort, threadIdx.x == 0,
+                               reinterpret_cast<const char*>(a.gsw), (uint32_t)n * kpl, 0};
+
+    char* pbase = smem + Plan::pair_off + (size_t)pr * Plan::pair;
+    StepCtx<R, PARTS, 1> St;
+    St.tw = hot_twiddles<R>(tables);
+    St.acc = reinterpret_cast<int32_t*>(pbase);
+    St.s[0] = scratch_at<R>(pbase + Plan::acc + h * Plan::half_scratch);
+    cpx<R>* peer_inbox = reinterpret_cast<cpx<R>*>(pbase + Plan::acc + (1 - h) * Plan::half_scratch);
+    St.t = t;
+    St.bar_id = 1 + 2 * pr + h;
+    const int pair_bar = 1 + 2 * PAIRS + pr;
+    St.Bgbit = kp.Bgbit;
+    St.split = kp.split;
+    St.offset = kp.offset;
+
+    // half h owns accumulator polynomial h
+    int32_t* mine = St.acc + h * kN;
+    if (a.acc_in) {
+        const int32_t* src = a.acc_in + (size_t)c * 2 * kN + h * kN;
+        for (int i = t; i < kN; i += 64) mine[i] = src[i];
+    } else {
+        const int32_t* xs = a.x + (size_t)c * (n + 1);
+        const int barb = mod_switch_2n(xs[n]);
+        for (int i = t; i < kN; i += 64)
+            mine[i] = h == 0 ? 0 : test_vector_coef(a, c, barb, i);
+    }
+    group_sync(St.bar_id);
+    const int32_t* bara = a.bara ? a.bara + (size_t)c * n : nullptr;
+    const int32_t* xs = a.x ? a.x + (size_t)c * (n + 1) : nullptr;
+    int a_next = bara ? bara[0] : mod_switch_2n(xs[0]);
+#pragma unroll 1
+    for (int i = 0; i < n; ++i) {
+        const int ai = a_next;
+        if (i + 1 < n) a_next = bara ? bara[i + 1] : mod_switch_2n(xs[i + 1]);
+        keys.row0 = (uint32_t)i * kpl;
+        if (ai == 0) {  // tfhe_blindRotate_FFT.cpp:114 -- this half's rows still pass through
+            for (int p = h * L; p < h * L + L; ++p) {
+                keys.acquire(p);
+                keys.release(p);
+            }
+            continue;
+        }
+        if (h == 0) ep_step_half<R, PARTS, L, 0>(St, keys, ai, peer_inbox, pair_bar);
+        else ep_step_half<R, PARTS, L, 1>(St, keys, ai, peer_inbox, pair_bar);
+    }
+    if (keys.producer) {
+        keys.issue_through(keys.total - 1);  // rows of a skipped last step
+        keys.drain();
+    }
+    pair_sync(pair_bar);  // both polynomials final
+    if (a.acc_out) {
+        int32_t* dst = a.acc_out + (size_t)c * 2 * kN + h * kN;
+        for (int i = t; i < kN; i += 64) dst[i] = mine[i];
+    }
+    if (a.lwe_out) {
+        // tLweExtractLweSample: a'_0 = a_0, a'_j = -a_{N-j}, b' = b_0
+        int32_t* dst = a.lwe_out + (size_t)c * (kN + 1);
+        const int tt = h * 64 + t;
+        for (int i = tt; i < kN; i += 128)
+            dst[i] = i == 0 ? St.acc[0] : (int32_t)(0u - (uint32_t)St.acc[kN - i]);
+        if (tt == 0) dst[kN] = St.acc[kN];
     }
 }
 
@@ -865,14 +1191,33 @@ uint32_t decomp_offset(int l, int Bgbit) {
     return o * (uint32_t)(1 << (Bgbit - 1));
 }
 
-template <typename R, int PARTS, int MODE, int GROUPS, int L>
-cudaError_t launch_ep_t(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
-    if (a.count <= 0) return cudaSuccess;
+KParams make_kparams(const DevParams& P) {
     KParams kp;
     kp.n = P.n;
     kp.Bgbit = P.Bgbit;
     kp.split = P.split_bits;
     kp.offset = decomp_offset(P.l, P.Bgbit);
+    return kp;
+}
+
+// The blind-rotation arguments of items [off, off + cnt) of a batch.
+EpArgs slice_blind_rotate(const DevParams& P, const EpArgs& a, int off, int cnt) {
+    EpArgs b = a;
+    const size_t o = (size_t)off;
+    if (a.acc_in) b.acc_in = a.acc_in + o * 2 * kN;
+    if (a.acc_out) b.acc_out = a.acc_out + o * 2 * kN;
+    if (a.bara) b.bara = a.bara + o * P.n;
+    if (a.x) b.x = a.x + o * (P.n + 1);
+    if (a.lwe_out) b.lwe_out = a.lwe_out + o * (kN + 1);
+    if (a.tv) b.tv = a.tv + o * a.tv_stride;
+    b.count = cnt;
+    return b;
+}
+
+template <typename R, int PARTS, int MODE, int GROUPS, int L>
+cudaError_t launch_ep_t(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
+    if (a.count <= 0) return cudaSuccess;
+    const KParams kp = make_kparams(P);
     const size_t smem = SmemPlan<R, (L > PARTS ? L : PARTS)>::total(GROUPS);
     auto kern = k_external_product<R, PARTS, MODE, GROUPS, L>;
     cudaError_t e = set_smem(kern, smem);
@@ -882,15 +1227,10 @@ cudaError_t launch_ep_t(const DevParams& P, const Tables& T, const EpArgs& a, cu
     return cudaGetLastError();
 }
 
-template <typename R, int PARTS, int GROUPS, int L, bool INLINE>
+template <typename R, int PARTS, int GROUPS, int L, bool INLINE, int S = 4>
 cudaError_t launch_ring_t(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
-    constexpr int S = 4;
     if (a.count <= 0) return cudaSuccess;
-    KParams kp;
-    kp.n = P.n;
-    kp.Bgbit = P.Bgbit;
-    kp.split = P.split_bits;
-    kp.offset = decomp_offset(P.l, P.Bgbit);
+    const KParams kp = make_kparams(P);
     using Plan = RingPlan<R, PARTS, GROUPS, L, S>;
     auto kern = k_blind_rotate_ring<R, PARTS, GROUPS, L, S, INLINE>;
     cudaError_t e = set_smem(kern, Plan::total);
@@ -898,6 +1238,49 @@ cudaError_t launch_ring_t(const DevParams& P, const Tables& T, const EpArgs& a, 
     const int grid = (a.count + GROUPS - 1) / GROUPS;
     kern<<<grid, 64 * GROUPS + (INLINE ? 0 : 32), Plan::total, st>>>(kp, T, a);
     return cudaGetLastError();
+}
+
+template <typename R, int PARTS, int PAIRS, int L, int S>
+cudaError_t launch_pair_t(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
+    if (a.count <= 0) return cudaSuccess;
+    const KParams kp = make_kparams(P);
+    using Plan = PairPlan<R, PARTS, PAIRS, L, S>;
+    auto kern = k_blind_rotate_pair<R, PARTS, PAIRS, L, S>;
+    cudaError_t e = set_smem(kern, Plan::total);
+    if (e != cudaSuccess) return e;
+    const int grid = (a.count + PAIRS - 1) / PAIRS;
+    kern<<<grid, 128 * PAIRS, Plan::total, st>>>(kp, T, a);
+    return cudaGetLastError();
+}
+
+// split-FP32 pair kernel with `per_cta` (1..3) ciphertexts per CTA
+template <int L>
+cudaError_t launch_pair_fp32(const DevParams& P, const Tables& T, const EpArgs& a, int per_cta,
+                             cudaStream_t st) {
+    // a 4-row ring: deeper rings (6, 8 rows) measured slower, the shared
+    // memory they take comes out of the L1 cache
+    if (per_cta <= 1) return launch_pair_t<float, 2, 1, L, 4>(P, T, a, st);
+    if (per_cta == 2) return launch_pair_t<float, 2, 2, L, 4>(P, T, a, st);
+    return launch_pair_t<float, 2, 3, L, 4>(P, T, a, st);
+}
+
+// Automatic shape of a split-FP32 blind rotation over `count` ciphertexts:
+// whole waves of six ciphertexts per SM on the shared-ring kernel; a
+// remainder of at most three per SM on the pair kernel (two halves per
+// ciphertext, about half the time per ciphertext), so the last partial wave
+// takes half a wave; a larger remainder as one more ring wave.
+template <int L>
+cudaError_t launch_auto_fp32(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
+    const int wave = 6 * kSmCount;
+    const int full = (a.count / wave) * wave;
+    const int rest = a.count - full;
+    if (rest == 0 || rest > 3 * kSmCount) return launch_ring_t<float, 2, 6, L, true>(P, T, a, st);
+    if (full) {
+        cudaError_t e = launch_ring_t<float, 2, 6, L, true>(P, T, slice_blind_rotate(P, a, 0, full), st);
+        if (e != cudaSuccess) return e;
+    }
+    const int per_cta = (rest + kSmCount - 1) / kSmCount;
+    return launch_pair_fp32<L>(P, T, slice_blind_rotate(P, a, full, rest), per_cta, st);
 }
 
 // FP64: ~250 registers per thread and 2 x L exchange buffers of 9 KB per
@@ -918,22 +1301,17 @@ cudaError_t launch_ep_l(const DevParams& P, Form f, EpMode mode, const Tables& T
     case kEpPlain: return launch_ep_t<float, 2, kEpPlain, 4, L>(P, T, a, st);
     case kEpMuxRotate: return launch_ep_t<float, 2, kEpMuxRotate, 4, L>(P, T, a, st);
     default:
-        if (groups == 0) {
-            // automatic: a batch that fills every SM with 6 ciphertexts uses
-            // the shared-ring kernel; smaller batches are spread over more
-            // SMs (fewer ciphertexts per CTA, key rows from L2) for latency
-            const int per_sm = (a.count + kSmCount - 1) / kSmCount;
-            if (per_sm >= 6) return launch_ring_t<float, 2, 6, L, true>(P, T, a, st);
-            if (per_sm == 1) return launch_ep_t<float, 2, kEpBlindRotate, 1, L>(P, T, a, st);
-            if (per_sm == 2) return launch_ep_t<float, 2, kEpBlindRotate, 2, L>(P, T, a, st);
-            return launch_ep_t<float, 2, kEpBlindRotate, 4, L>(P, T, a, st);
-        }
+        if (groups == 0) return launch_auto_fp32<L>(P, T, a, st);
         // 1, 2, 4: L2-direct key reads; 5: shared ring fed by a producer
-        // warp; 6: shared ring fed in line by one consumer thread
+        // warp; 6, 7, 8: shared ring fed in line by one consumer thread;
+        // 11, 12, 13: pair kernel with 1, 2, 3 ciphertexts per CTA
+        if (groups >= 11 && groups <= 13) return launch_pair_fp32<L>(P, T, a, groups - 10, st);
         if (groups == 1) return launch_ep_t<float, 2, kEpBlindRotate, 1, L>(P, T, a, st);
         if (groups == 2) return launch_ep_t<float, 2, kEpBlindRotate, 2, L>(P, T, a, st);
         if (groups == 4) return launch_ep_t<float, 2, kEpBlindRotate, 4, L>(P, T, a, st);
         if (groups == 5) return launch_ring_t<float, 2, 5, L, false>(P, T, a, st);
+        if (groups == 7) return launch_ring_t<float, 2, 7, L, true>(P, T, a, st);
+        if (groups == 8) return launch_ring_t<float, 2, 8, L, true>(P, T, a, st);
         return launch_ring_t<float, 2, 6, L, true>(P, T, a, st);
     }
 }
@@ -966,13 +1344,18 @@ static void sincos_2pi_frac(long k, long M, double* c, double* s) {
 }
 
 void make_twiddles_host(double* h) {
-    // layout of Tables: [q][t] W^(tq) | [q][j] W^(8jq) | psi^x, W = e^{2 pi i/512}
+    // layout of Tables: [q][t] W^(tq) | [q][j] W^(8jq) | [q][t] psi^t W^(tq) | psi^x,
+    // W = e^{2 pi i/512}, psi = e^{pi i/1024}
     for (int q = 0; q < 8; ++q)
         for (int t = 0; t < 64; ++t)
             sincos_2pi_frac(t * q, 512, &h[2 * (kTabA + q * 64 + t)], &h[2 * (kTabA + q * 64 + t) + 1]);
     for (int q = 0; q < 8; ++q)
         for (int j = 0; j < 8; ++j)
             sincos_2pi_frac(8 * j * q, 512, &h[2 * (kTabB + q * 8 + j)], &h[2 * (kTabB + q * 8 + j) + 1]);
+    // psi^t W^(tq) = e^{2 pi i (t + 4 t q) / 2048}
+    for (int q = 0; q < 8; ++q)
+        for (int t = 0; t < 64; ++t)
+            sincos_2pi_frac(t + 4 * t * q, 2048, &h[2 * (kTabT + q * 64 + t)], &h[2 * (kTabT + q * 64 + t) + 1]);
     for (int x = 0; x < 512; ++x)
         sincos_2pi_frac(x, 2048, &h[2 * (kTabPsi + x)], &h[2 * (kTabPsi + x) + 1]);
 }

@@ -139,6 +139,19 @@ tfhe_gpu_status run_bootstrap_woks(tfhe_gpu_ctx* ctx, const int32_t* x, int32_t 
     return TFHE_GPU_OK;
 }
 
+// combine -> blind rotation + extraction -> key switch, with the gate
+// combinations in x (count x (n+1)) and the extracted samples in u
+// (count x (kN+1)), both device buffers of the caller.
+tfhe_gpu_status run_gates_in(tfhe_gpu_ctx* ctx, const int32_t* gates, int32_t uniform_gate,
+                             int32_t* out, const int32_t* ca, const int32_t* cb, int32_t count,
+                             int32_t form, int32_t* x, int32_t* u, cudaStream_t st) {
+    CK(ctx, launch_gate_combine(ctx->dp, gates, uniform_gate, ca, cb, x, count, st));
+    const int32_t mu = tfhe_client_mod_switch_to_torus32(1, 8);
+    RET(run_bootstrap_woks(ctx, x, mu, u, count, form, st));
+    CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, u, out, count, st));
+    return TFHE_GPU_OK;
+}
+
 tfhe_gpu_status run_gates(tfhe_gpu_ctx* ctx, const int32_t* gates, int32_t uniform_gate,
                           int32_t* out, const int32_t* ca, const int32_t* cb, int32_t count,
                           int32_t form, cudaStream_t st) {
@@ -149,12 +162,7 @@ tfhe_gpu_status run_gates(tfhe_gpu_ctx* ctx, const int32_t* gates, int32_t unifo
     void *x = nullptr, *u = nullptr;
     RET(ensure_scratch(ctx, 0, (size_t)count * (n + 1) * sizeof(int32_t), &x));
     RET(ensure_scratch(ctx, 1, (size_t)count * (nk + 1) * sizeof(int32_t), &u));
-    CK(ctx, launch_gate_combine(ctx->dp, gates, uniform_gate, ca, cb, (int32_t*)x, count, st));
-    const int32_t mu = tfhe_client_mod_switch_to_torus32(1, 8);
-    RET(run_bootstrap_woks(ctx, (const int32_t*)x, mu, (int32_t*)u, count, form, st));
-    CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, (const int32_t*)u, out, count,
-                             st));
-    return TFHE_GPU_OK;
+    return run_gates_in(ctx, gates, uniform_gate, out, ca, cb, count, form, (int32_t*)x, (int32_t*)u, st);
 }
 
 }  // namespace
@@ -278,7 +286,7 @@ tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form for
                                             int32_t groups) {
     if (!ctx || !form_ok(form)) return TFHE_GPU_BAD_PARAM;
     const bool ok = form == TFHE_GPU_FP64 ? (groups == 3 || groups == 4)
-                                          : (groups >= 0 && groups <= 6 && groups != 3);
+                                          : ((groups >= 0 && groups <= 8 && groups != 3) || (groups >= 11 && groups <= 13));
     if (!ok) return fail(ctx, TFHE_GPU_BAD_PARAM, "unsupported groups per CTA for this form");
     ctx->groups_per_cta[form] = groups;
     return TFHE_GPU_OK;
@@ -372,6 +380,52 @@ tfhe_gpu_status tfhe_gpu_upload_keyswitch_key(tfhe_gpu_ctx* ctx, const int32_t* 
     CK(ctx, cudaMemcpy2D(ctx->d_ks, stride * sizeof(int32_t), ks, (n + 1) * sizeof(int32_t),
                          (n + 1) * sizeof(int32_t), rows, cudaMemcpyHostToDevice));
     return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_gate_keyset(tfhe_gpu_ctx* ctx, int32_t* lwe_key, int32_t* tlwe_key,
+                                     int32_t* ks, int32_t* bk, uint32_t form_mask) {
+    CHECK_CTX(ctx);
+    if (!lwe_key || !tlwe_key || !ks || (form_mask & ~3u) || !form_mask)
+        return fail(ctx, TFHE_GPU_BAD_PARAM, "keyset args");
+    const tfhe_params& P = ctx->P;
+    const size_t words = (size_t)P.n * (P.k + 1) * P.l * (P.k + 1) * P.N;
+    std::vector<int32_t> own;
+    int32_t* h_bk = bk;
+    if (!h_bk) {
+        own.resize(words);
+        h_bk = own.data();
+    }
+    // every random value on the host, in the reference's order
+    RET(gate_keyset_host(&P, lwe_key, tlwe_key, ks, h_bk, false));
+    int32_t *d_bk = nullptr, *d_keys = nullptr;
+    tfhe_gpu_status s = TFHE_GPU_OK;
+    cudaError_t e = cudaMalloc(&d_bk, words * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&d_keys, (size_t)(P.k * P.N + P.n) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMemcpy(d_bk, h_bk, words * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(d_keys, tlwe_key, (size_t)P.k * P.N * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(d_keys + P.k * P.N, lwe_key, (size_t)P.n * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_tgsw_finish(ctx->dp, d_bk, d_keys, d_keys + P.k * P.N, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) s = cuda_fail(ctx, e, "bootstrapping key on the device");
+    if (s == TFHE_GPU_OK) s = build_bk_forms(ctx, d_bk, form_mask);
+    if (s == TFHE_GPU_OK && bk) {
+        e = cudaMemcpy(bk, d_bk, words * sizeof(int32_t), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) s = cuda_fail(ctx, e, "copy bootstrapping key back");
+    }
+    cudaFree(d_bk);
+    cudaFree(d_keys);
+    if (s == TFHE_GPU_OK) s = tfhe_gpu_upload_keyswitch_key(ctx, ks);
+    return s;
+}
+
+tfhe_gpu_status tfhe_gpu_upload_cloud_key(tfhe_gpu_ctx* ctx, const int32_t* bk, const int32_t* ks,
+                                          uint32_t form_mask) {
+    CHECK_CTX(ctx);
+    if (!bk || !ks) return fail(ctx, TFHE_GPU_BAD_PARAM, "bk/ks");
+    RET(tfhe_gpu_upload_bootstrapping_key(ctx, bk, form_mask));
+    return tfhe_gpu_upload_keyswitch_key(ctx, ks);
 }
 
 tfhe_gpu_status tfhe_gpu_tgsw_to_fft(tfhe_gpu_ctx* ctx, const int32_t* tgsw, void* out,
@@ -529,6 +583,37 @@ tfhe_gpu_status tfhe_gpu_tfhe_bootstrap_FFT(tfhe_gpu_ctx* ctx, int32_t* out, con
     return TFHE_GPU_OK;
 }
 
+tfhe_gpu_status tfhe_gpu_bootstrap_tv(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* x,
+                                      const int32_t* tv, int32_t tv_stride, int32_t count,
+                                      tfhe_gpu_form form, int32_t keyswitch, void* stream) {
+    CHECK_CTX(ctx);
+    RET(need_bk(ctx, form));
+    if (keyswitch && !ctx->d_ks) return fail(ctx, TFHE_GPU_NO_KEY, "key-switching key not uploaded");
+    if (count < 0 || (count && (!out || !x || !tv)) || (tv_stride != 0 && tv_stride != ctx->P.N))
+        return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    if (count == 0) return TFHE_GPU_OK;
+    cudaStream_t st = pick(ctx, stream);
+    int32_t* u = out;
+    if (keyswitch) {
+        void* scratch;
+        RET(ensure_scratch(ctx, 1, (size_t)count * (ctx->P.k * ctx->P.N + 1) * sizeof(int32_t), &scratch));
+        u = (int32_t*)scratch;
+    }
+    EpArgs a{};
+    a.err = ctx->d_err;
+    a.x = x;
+    a.tv = tv;
+    a.tv_stride = tv_stride;
+    a.lwe_out = u;
+    a.gsw = ctx->d_bk[form];
+    a.count = count;
+    CK(ctx, launch_external_product(ctx->dp, (Form)form, kEpBlindRotate, ctx->tables, a,
+                                    ctx->groups_per_cta[form], st));
+    if (keyswitch)
+        CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, u, out, count, st));
+    return TFHE_GPU_OK;
+}
+
 tfhe_gpu_status tfhe_gpu_bootsGate(tfhe_gpu_ctx* ctx, int32_t gate, int32_t* out,
                                    const int32_t* ca, const int32_t* cb, int32_t count,
                                    tfhe_gpu_form form, void* stream) {
@@ -597,6 +682,174 @@ tfhe_gpu_status tfhe_gpu_bootsGates_host(tfhe_gpu_ctx* ctx, const int32_t* gates
     CK(ctx, cudaMemcpyAsync(d_cb, cb, lwe_bytes, cudaMemcpyHostToDevice, st));
     if (gates) CK(ctx, cudaMemcpyAsync(d_g, gates, count * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     RET(run_gates(ctx, (const int32_t*)d_g, uniform_gate, d_out, d_ca, d_cb, count, form, st));
+    CK(ctx, cudaMemcpyAsync(out, d_out, lwe_bytes, cudaMemcpyDeviceToHost, st));
+    CK(ctx, cudaStreamSynchronize(st));
+    return check_device_status(ctx);
+}
+
+// ---- CUDA graph of the gate pipeline, launch-shape autotuner -----------
+
+struct tfhe_gpu_graph {
+    tfhe_gpu_ctx* ctx = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int32_t* x = nullptr;  // private scratch: the graph's pointers must stay valid
+    int32_t* u = nullptr;
+    int32_t kernels = 0;
+};
+
+void tfhe_gpu_graph_destroy(tfhe_gpu_graph* g) {
+    if (!g) return;
+    if (g->ctx) set_device(g->ctx);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    cudaFree(g->x);
+    cudaFree(g->u);
+    delete g;
+}
+
+tfhe_gpu_status tfhe_gpu_graph_gates_create(tfhe_gpu_ctx* ctx, const int32_t* gates,
+                                            int32_t uniform_gate, int32_t* out, const int32_t* ca,
+                                            const int32_t* cb, int32_t count, tfhe_gpu_form form,
+                                            tfhe_gpu_graph** result) {
+    CHECK_CTX(ctx);
+    if (!result || count <= 0 || !out || !ca || !cb || !form_ok(form) ||
+        (!gates && (uniform_gate < 0 || uniform_gate > 9)))
+        return fail(ctx, TFHE_GPU_BAD_PARAM, "graph args");
+    *result = nullptr;
+    RET(need_bk(ctx, form));
+    if (!ctx->d_ks) return fail(ctx, TFHE_GPU_NO_KEY, "key-switching key not uploaded");
+    const int n = ctx->P.n, nk = ctx->P.k * ctx->P.N;
+    tfhe_gpu_graph* g = new tfhe_gpu_graph();
+    g->ctx = ctx;
+    cudaStream_t cs = nullptr;
+    auto bail = [&](tfhe_gpu_status s) {
+        if (cs) cudaStreamDestroy(cs);
+        tfhe_gpu_graph_destroy(g);
+        return s;
+    };
+    cudaError_t e = cudaMalloc(&g->x, (size_t)count * (n + 1) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&g->u, (size_t)count * (nk + 1) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "graph buffers"));
+    // one eager run: kernel attributes set, errors surface before capture
+    tfhe_gpu_status s = run_gates_in(ctx, gates, uniform_gate, out, ca, cb, count, form, g->x, g->u, cs);
+    if (s == TFHE_GPU_OK && (e = cudaStreamSynchronize(cs)) != cudaSuccess) s = cuda_fail(ctx, e, "eager run");
+    if (s == TFHE_GPU_OK) s = check_device_status(ctx);
+    if (s != TFHE_GPU_OK) return bail(s);
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "begin capture"));
+    s = run_gates_in(ctx, gates, uniform_gate, out, ca, cb, count, form, g->x, g->u, cs);
+    e = cudaStreamEndCapture(cs, &g->graph);
+    if (s != TFHE_GPU_OK) return bail(s);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "end capture"));
+    e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "instantiate"));
+    size_t nodes = 0;
+    if (cudaGraphGetNodes(g->graph, nullptr, &nodes) == cudaSuccess && nodes) {
+        std::vector<cudaGraphNode_t> list(nodes);
+        cudaGraphGetNodes(g->graph, list.data(), &nodes);
+        for (cudaGraphNode_t nd : list) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++g->kernels;
+        }
+    }
+    cudaStreamDestroy(cs);
+    *result = g;
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_graph_launch(tfhe_gpu_graph* g, void* stream) {
+    if (!g || !g->exec) return TFHE_GPU_BAD_PARAM;
+    CHECK_CTX(g->ctx);
+    CK(g->ctx, cudaGraphLaunch(g->exec, pick(g->ctx, stream)));
+    return TFHE_GPU_OK;
+}
+
+int32_t tfhe_gpu_graph_kernel_count(const tfhe_gpu_graph* g) { return g ? g->kernels : 0; }
+
+tfhe_gpu_status tfhe_gpu_autotune(tfhe_gpu_ctx* ctx, tfhe_gpu_form form, int32_t count,
+                                  int32_t* best_shape, float* best_ms) {
+    CHECK_CTX(ctx);
+    if (!form_ok(form) || count <= 0) return fail(ctx, TFHE_GPU_BAD_PARAM, "autotune args");
+    RET(need_bk(ctx, form));
+    static const int kFp32[] = {0, 6, 7, 5, 13, 12, 4, 2, 1};
+    static const int kFp64[] = {3, 4};
+    const int* cand = form == TFHE_GPU_FP64 ? kFp64 : kFp32;
+    const int ncand = form == TFHE_GPU_FP64 ? 2 : 9;
+    const int n = ctx->P.n, nk = ctx->P.k * ctx->P.N;
+    // synthetic inputs: uniform Torus32 samples (a_i = 0 would skip steps)
+    std::vector<int32_t> hx((size_t)count * (n + 1));
+    uint64_t st = 0x9E3779B97F4A7C15ull;
+    for (auto& v : hx) {
+        st ^= st << 13;
+        st ^= st >> 7;
+        st ^= st << 17;
+        v = (int32_t)(uint32_t)(st >> 16);
+    }
+    int32_t *x = nullptr, *u = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const int keep = ctx->groups_per_cta[form];
+    tfhe_gpu_status s = TFHE_GPU_OK;
+    cudaError_t e = cudaMalloc(&x, hx.size() * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&u, (size_t)count * (nk + 1) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMemcpy(x, hx.data(), hx.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) s = cuda_fail(ctx, e, "autotune buffers");
+    int best = keep;
+    float best_t = 0;
+    for (int i = 0; s == TFHE_GPU_OK && i < ncand; ++i) {
+        const int shape = cand[i];
+        if (shape >= 1 && shape <= 2 && count > 2 * kSmCount) continue;  // far slower than the rest
+        ctx->groups_per_cta[form] = shape;
+        const int32_t mu = tfhe_client_mod_switch_to_torus32(1, 8);
+        float t_min = 0;
+        for (int rep = 0; rep < 3 && s == TFHE_GPU_OK; ++rep) {
+            cudaEventRecord(e0, ctx->stream);
+            s = run_bootstrap_woks(ctx, x, mu, u, count, form, ctx->stream);
+            cudaEventRecord(e1, ctx->stream);
+            if (s == TFHE_GPU_OK && (e = cudaEventSynchronize(e1)) != cudaSuccess) s = cuda_fail(ctx, e, "autotune");
+            if (s == TFHE_GPU_OK) s = check_device_status(ctx);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0 && (t_min == 0 || ms < t_min)) t_min = ms;  // first run warms up
+        }
+        if (s == TFHE_GPU_OK && (best_t == 0 || t_min < best_t)) {
+            best_t = t_min;
+            best = shape;
+        }
+    }
+    ctx->groups_per_cta[form] = s == TFHE_GPU_OK ? best : keep;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(x);
+    cudaFree(u);
+    if (s != TFHE_GPU_OK) return s;
+    if (best_shape) *best_shape = best;
+    if (best_ms) *best_ms = best_t;
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_gpu_bootsMUX_host(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* a,
+                                       const int32_t* b, const int32_t* c, int32_t count,
+                                       tfhe_gpu_form form) {
+    CHECK_CTX(ctx);
+    if (count < 0 || (count && (!out || !a || !b || !c))) return fail(ctx, TFHE_GPU_BAD_PARAM, "args");
+    if (count == 0) return TFHE_GPU_OK;
+    const size_t lwe_bytes = (size_t)count * (ctx->P.n + 1) * sizeof(int32_t);
+    void* d_io = nullptr;
+    RET(ensure_scratch(ctx, 3, 4 * lwe_bytes, &d_io));
+    char* base = (char*)d_io;
+    int32_t* d_a = (int32_t*)base;
+    int32_t* d_b = (int32_t*)(base + lwe_bytes);
+    int32_t* d_c = (int32_t*)(base + 2 * lwe_bytes);
+    int32_t* d_out = (int32_t*)(base + 3 * lwe_bytes);
+    cudaStream_t st = ctx->stream;
+    CK(ctx, cudaMemcpyAsync(d_a, a, lwe_bytes, cudaMemcpyHostToDevice, st));
+    CK(ctx, cudaMemcpyAsync(d_b, b, lwe_bytes, cudaMemcpyHostToDevice, st));
+    CK(ctx, cudaMemcpyAsync(d_c, c, lwe_bytes, cudaMemcpyHostToDevice, st));
+    RET(tfhe_gpu_bootsMUX(ctx, d_out, d_a, d_b, d_c, count, form, st));
     CK(ctx, cudaMemcpyAsync(out, d_out, lwe_bytes, cudaMemcpyDeviceToHost, st));
     CK(ctx, cudaStreamSynchronize(st));
     return check_device_status(ctx);

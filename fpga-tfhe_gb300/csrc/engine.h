@@ -8,6 +8,10 @@
 
 namespace tfhe_gb300 {
 
+// Streaming multiprocessors of a GB300 (two dies of 76): launch shapes are
+// sized in waves of this many CTAs.
+constexpr int kSmCount = 152;
+
 // Precision forms of the transform.
 enum Form {
     kFormFp64 = 0,       // FP64 transform and product, truncating conversion
@@ -72,6 +76,10 @@ struct EpArgs {
     size_t gsw_stride;
     int count;
     int32_t* err;  // device status word: set to 3 (timeout) by a bounded wait
+    // kEpBlindRotate from x: test vector polynomial (N int32, item c at
+    // tv + c * tv_stride) instead of the constant mu; nullptr = constant mu
+    const int32_t* tv;
+    int32_t tv_stride;
 };
 
 cudaError_t launch_external_product(const DevParams& P, Form f, EpMode mode,
@@ -110,4 +118,21 @@ cudaError_t launch_keyswitch(const DevParams& P, const int32_t* ks,
                              int32_t row_stride, const int32_t* in,
                              int32_t* out, int count, cudaStream_t st);
 
+// Finish n TGSW encryptions whose rows hold masks a and noise b = e (host
+// RNG, exact order): b += sum_i a_i * s_i (negacyclic, TLWE key s, N k
+// int32) and the gadget term lwe_key[row / kpl] * 2^(32 - (j+1) Bgbit) on
+// coefficient 0 of polynomial i of row (i, j).  bk: device, n x kpl x
+// (k+1) x N int32, in place.
+cudaError_t launch_tgsw_finish(const DevParams& P, int32_t* bk, const int32_t* tlwe_key,
+                               const int32_t* lwe_key, cudaStream_t st);
+
+}  // namespace tfhe_gb300
+
+// Host key generation (keygen.cpp).  With bk_products false the rows of the
+// bootstrapping key are left with their masks and noise only, for
+// launch_tgsw_finish; the RNG stream is the same either way.
+#include "../../include/tfhe_gpu.h"
+namespace tfhe_gb300 {
+tfhe_gpu_status gate_keyset_host(const tfhe_params* P, int32_t* lwe_key, int32_t* tlwe_key,
+                                 int32_t* ks, int32_t* bk, bool bk_products);
 }  // namespace tfhe_gb300

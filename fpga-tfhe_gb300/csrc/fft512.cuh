@@ -58,6 +58,23 @@ constexpr int kScratchStride = 576;  // 512 + 512/8 padding
 
 __device__ __forceinline__ int spad(int p) { return p + (p >> 3); }
 
+// Shared-memory slot of point p in an exchange buffer, chosen so that every
+// access pattern of the three passes (A: p = t + 64q, B: p = 64(t/8) +
+// t%8 + 8r, C: p = 8t + r over the lanes t of a warp) is free of bank
+// conflicts.  FP32 (8-byte points, half-warp wavefronts): an XOR of the low
+// four bits with a function of p/16 -- padding would leave pass A with a
+// two-way conflict.  FP64 (16-byte points, quarter-warp wavefronts): one pad
+// slot every 8 points.
+template <typename R>
+__device__ __forceinline__ int slot(int p);
+template <>
+__device__ __forceinline__ int slot<float>(int p) {
+    const int k = p >> 4;
+    return p ^ ((k & 7) | ((k & 4) << 1));
+}
+template <>
+__device__ __forceinline__ int slot<double>(int p) { return spad(p); }
+
 // 8-point DFT, y_q = sum_r v_r w^{rq}, w = e^{S 2 pi i / 8}.
 template <int S, typename R>
 __device__ __forceinline__ void dft8(cpx<R> (&v)[8]) {
@@ -123,21 +140,21 @@ __device__ __forceinline__ void fft512_forward(cpx<R> (&v)[8], const FftScratch<
 #pragma unroll
     for (int q = 1; q < 8; ++q) v[q] = cmul(v[q], tw.a[q * 64 + t]);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) s.b0[spad(t + 64 * q)] = v[q];
+    for (int q = 0; q < 8; ++q) s.b0[slot<R>(t + 64 * q)] = v[q];
     group_sync(bar_id);
     // pass B
     const int b = t >> 3, j = t & 7;
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = s.b0[spad(64 * b + j + 8 * r)];
+    for (int r = 0; r < 8; ++r) v[r] = s.b0[slot<R>(64 * b + j + 8 * r)];
     dft8<1>(v);
 #pragma unroll
     for (int q = 1; q < 8; ++q) v[q] = cmul(v[q], tw.b[q * 8 + j]);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) s.b1[spad(64 * b + j + 8 * q)] = v[q];
+    for (int q = 0; q < 8; ++q) s.b1[slot<R>(64 * b + j + 8 * q)] = v[q];
     group_sync(bar_id);
     // pass C
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = s.b1[spad(8 * t + r)];
+    for (int r = 0; r < 8; ++r) v[r] = s.b1[slot<R>(8 * t + r)];
     dft8<1>(v);
 }
 
@@ -149,23 +166,23 @@ __device__ __forceinline__ void fft512_inverse(cpx<R> (&v)[8], const FftScratch<
     // pass C'
     dft8<-1>(v);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) s.b0[spad(8 * t + q)] = v[q];
+    for (int q = 0; q < 8; ++q) s.b0[slot<R>(8 * t + q)] = v[q];
     group_sync(bar_id);
     // pass B'
     const int b = t >> 3, j = t & 7;
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-        v[r] = s.b0[spad(64 * b + j + 8 * r)];
+        v[r] = s.b0[slot<R>(64 * b + j + 8 * r)];
         if (r) v[r] = cmulc(v[r], tw.b[r * 8 + j]);
     }
     dft8<-1>(v);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) s.b1[spad(64 * b + j + 8 * q)] = v[q];
+    for (int q = 0; q < 8; ++q) s.b1[slot<R>(64 * b + j + 8 * q)] = v[q];
     group_sync(bar_id);
     // pass A'
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-        v[r] = s.b1[spad(t + 64 * r)];
+        v[r] = s.b1[slot<R>(t + 64 * r)];
         if (r) v[r] = cmulc(v[r], tw.a[r * 64 + t]);
     }
     dft8<-1>(v);
@@ -184,25 +201,25 @@ __device__ __forceinline__ void fft512_forward_multi(cpx<R> (&v)[NB][8], const F
 #pragma unroll
         for (int q = 1; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.a[q * 64 + t]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b0[spad(t + 64 * q)] = v[b][q];
+        for (int q = 0; q < 8; ++q) s[b].b0[slot<R>(t + 64 * q)] = v[b][q];
     }
     group_sync(bar_id);
     const int hb = t >> 3, j = t & 7;
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b0[spad(64 * hb + j + 8 * r)];
+        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b0[slot<R>(64 * hb + j + 8 * r)];
         dft8<1>(v[b]);
 #pragma unroll
         for (int q = 1; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.b[q * 8 + j]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b1[spad(64 * hb + j + 8 * q)] = v[b][q];
+        for (int q = 0; q < 8; ++q) s[b].b1[slot<R>(64 * hb + j + 8 * q)] = v[b][q];
     }
     group_sync(bar_id);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b1[spad(8 * t + r)];
+        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b1[slot<R>(8 * t + r)];
         dft8<1>(v[b]);
     }
 }
@@ -214,7 +231,7 @@ __device__ __forceinline__ void fft512_inverse_multi(cpx<R> (&v)[NB][8], const F
     for (int b = 0; b < NB; ++b) {
         dft8<-1>(v[b]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b0[spad(8 * t + q)] = v[b][q];
+        for (int q = 0; q < 8; ++q) s[b].b0[slot<R>(8 * t + q)] = v[b][q];
     }
     group_sync(bar_id);
     const int hb = t >> 3, j = t & 7;
@@ -222,23 +239,131 @@ __device__ __forceinline__ void fft512_inverse_multi(cpx<R> (&v)[NB][8], const F
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-            v[b][r] = s[b].b0[spad(64 * hb + j + 8 * r)];
+            v[b][r] = s[b].b0[slot<R>(64 * hb + j + 8 * r)];
             if (r) v[b][r] = cmulc(v[b][r], tw.b[r * 8 + j]);
         }
         dft8<-1>(v[b]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b1[spad(64 * hb + j + 8 * q)] = v[b][q];
+        for (int q = 0; q < 8; ++q) s[b].b1[slot<R>(64 * hb + j + 8 * q)] = v[b][q];
     }
     group_sync(bar_id);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-            v[b][r] = s[b].b1[spad(t + 64 * r)];
+            v[b][r] = s[b].b1[slot<R>(t + 64 * r)];
             if (r) v[b][r] = cmulc(v[b][r], tw.a[r * 64 + t]);
         }
         dft8<-1>(v[b]);
     }
+}
+
+// ----------------------------------------------------------------------
+// Transforms with the negacyclic twist folded in.  Point x = t + 64r of a
+// thread is twisted by psi^x = psi^t c_r, c_r = psi^(64 r) = e^{i pi r/16}:
+// the compile-time c_r multiply the inputs, and psi^t, common to the
+// thread's radix-8 block, joins pass A's twiddles in the table
+// tw.a[q * 64 + t] = psi^t W^(t q) (q = 0..7).  The inverse mirrors it:
+// conj(psi^t W^(t r)) on pass A''s inputs, conj(c_q) on its outputs.  Same
+// number of roundings as a separate twist, and no psi^x loads.
+// ----------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ cpx<R> twist_c(int r) {
+    // e^{i pi r / 16}, r = 0..7
+    constexpr double kC[8][2] = {{1.0, 0.0},
+                                 {0.9807852804032304, 0.19509032201612825},
+                                 {0.9238795325112867, 0.3826834323650898},
+                                 {0.8314696123025452, 0.5555702330196022},
+                                 {0.7071067811865476, 0.7071067811865475},
+                                 {0.5555702330196023, 0.8314696123025452},
+                                 {0.38268343236508984, 0.9238795325112867},
+                                 {0.19509032201612833, 0.9807852804032304}};
+    return {(R)kC[r][0], (R)kC[r][1]};
+}
+
+// In: v[r] = untwisted folded point t + 64r.  Out: v[q] = position 8t + q
+// of the transform of the twisted sequence.  tw.a = psi^t W^(tq) table.
+template <int NB, typename R>
+__device__ __forceinline__ void fft512_forward_tw_multi(cpx<R> (&v)[NB][8], const FftScratch<R> (&s)[NB],
+                                                        const FftTwiddles<R>& tw, int t, int bar_id) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 1; r < 8; ++r) v[b][r] = cmul(v[b][r], twist_c<R>(r));
+        dft8<1>(v[b]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.a[q * 64 + t]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s[b].b0[slot<R>(t + 64 * q)] = v[b][q];
+    }
+    group_sync(bar_id);
+    const int hb = t >> 3, j = t & 7;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b0[slot<R>(64 * hb + j + 8 * r)];
+        dft8<1>(v[b]);
+#pragma unroll
+        for (int q = 1; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.b[q * 8 + j]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s[b].b1[slot<R>(64 * hb + j + 8 * q)] = v[b][q];
+    }
+    group_sync(bar_id);
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b1[slot<R>(8 * t + r)];
+        dft8<1>(v[b]);
+    }
+}
+
+// In: v[q] = position 8t + q.  Out: v[q] = 512 z[t + 64q] untwisted (times
+// psi^-(t + 64q)), not yet divided by 512.
+template <int NB, typename R>
+__device__ __forceinline__ void fft512_inverse_tw_multi(cpx<R> (&v)[NB][8], const FftScratch<R> (&s)[NB],
+                                                        const FftTwiddles<R>& tw, int t, int bar_id) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        dft8<-1>(v[b]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s[b].b0[slot<R>(8 * t + q)] = v[b][q];
+    }
+    group_sync(bar_id);
+    const int hb = t >> 3, j = t & 7;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            v[b][r] = s[b].b0[slot<R>(64 * hb + j + 8 * r)];
+            if (r) v[b][r] = cmulc(v[b][r], tw.b[r * 8 + j]);
+        }
+        dft8<-1>(v[b]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s[b].b1[slot<R>(64 * hb + j + 8 * q)] = v[b][q];
+    }
+    group_sync(bar_id);
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[b][r] = cmulc(s[b].b1[slot<R>(t + 64 * r)], tw.a[r * 64 + t]);
+        dft8<-1>(v[b]);
+#pragma unroll
+        for (int q = 1; q < 8; ++q) v[b][q] = cmulc(v[b][q], twist_c<R>(q));
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void fft512_forward_tw(cpx<R> (&v)[8], const FftScratch<R>& s,
+                                                  const FftTwiddles<R>& tw, int t, int bar_id) {
+    fft512_forward_tw_multi<1>(*reinterpret_cast<cpx<R>(*)[1][8]>(&v),
+                               *reinterpret_cast<const FftScratch<R>(*)[1]>(&s), tw, t, bar_id);
+}
+
+template <typename R>
+__device__ __forceinline__ void fft512_inverse_tw(cpx<R> (&v)[8], const FftScratch<R>& s,
+                                                  const FftTwiddles<R>& tw, int t, int bar_id) {
+    fft512_inverse_tw_multi<1>(*reinterpret_cast<cpx<R>(*)[1][8]>(&v),
+                               *reinterpret_cast<const FftScratch<R>(*)[1]>(&s), tw, t, bar_id);
 }
 
 // Frequency held at (thread t, register q) after the forward transform.

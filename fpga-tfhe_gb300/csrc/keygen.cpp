@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/tfhe_gpu.h"
+#include "engine.h"
 
 namespace {
 
@@ -77,8 +78,12 @@ int32_t tfhe_client_mod_switch_to_torus32(int32_t mu, int32_t Msize) {
     return (int32_t)(phase64 >> 32);
 }
 
-tfhe_gpu_status tfhe_client_gate_keyset(const tfhe_params* P, int32_t* lwe_key,
-                                        int32_t* tlwe_key, int32_t* ks, int32_t* bk) {
+}  // extern "C"
+
+namespace tfhe_gb300 {
+
+tfhe_gpu_status gate_keyset_host(const tfhe_params* P, int32_t* lwe_key, int32_t* tlwe_key,
+                                 int32_t* ks, int32_t* bk, bool bk_products) {
     if (!params_ok(P) || !lwe_key || !tlwe_key || !ks || !bk) return TFHE_GPU_BAD_PARAM;
     const int32_t n = P->n, N = P->N, k = P->k, l = P->l;
     const int32_t kpl = (k + 1) * l;
@@ -132,9 +137,10 @@ tfhe_gpu_status tfhe_client_gate_keyset(const tfhe_params* P, int32_t* lwe_key,
                 for (int32_t i = 0; i < k; ++i) {
                     int32_t* a = row + (size_t)i * N;
                     for (int32_t j = 0; j < N; ++j) a[j] = g_unif(g_gen);
-                    addmul_binary(N, b, tlwe_key + i * N, a);
+                    if (bk_products) addmul_binary(N, b, tlwe_key + i * N, a);
                 }
             }
+            if (!bk_products) continue;  // finished on the device (launch_tgsw_finish)
             for (int32_t i = 0; i <= k; ++i)
                 for (int32_t j = 0; j < l; ++j) {
                     int32_t* row = g + (size_t)(i * l + j) * (k + 1) * N;
@@ -143,6 +149,35 @@ tfhe_gpu_status tfhe_client_gate_keyset(const tfhe_params* P, int32_t* lwe_key,
                 }
         }
     }
+    return TFHE_GPU_OK;
+}
+
+}  // namespace tfhe_gb300
+
+extern "C" {
+
+tfhe_gpu_status tfhe_client_gate_keyset(const tfhe_params* P, int32_t* lwe_key,
+                                        int32_t* tlwe_key, int32_t* ks, int32_t* bk) {
+    return tfhe_gb300::gate_keyset_host(P, lwe_key, tlwe_key, ks, bk, true);
+}
+
+tfhe_gpu_status tfhe_client_test_vector(int32_t N, const int32_t* table, int32_t p, int32_t* tv) {
+    if (N <= 0 || p <= 0 || p > N || !table || !tv) return TFHE_GPU_BAD_PARAM;
+    // coefficient j belongs to the message whose phase window m/(2p) +-
+    // 1/(4p) holds j/(2N); the top half-window wraps (negacyclically) onto
+    // message 0 from below, hence -table[0] there
+    for (int32_t j = 0; j < N; ++j) {
+        const int64_t m = ((int64_t)j * p + N / 2) / N;
+        tv[j] = m < p ? table[m] : (int32_t)(0u - (uint32_t)table[0]);
+    }
+    return TFHE_GPU_OK;
+}
+
+tfhe_gpu_status tfhe_client_encrypt_phases(const tfhe_params* P, const int32_t* mu,
+                                           int32_t count, const int32_t* lwe_key, int32_t* out) {
+    if (!params_ok(P) || count < 0 || (count && (!mu || !lwe_key || !out))) return TFHE_GPU_BAD_PARAM;
+    for (int32_t c = 0; c < count; ++c)
+        lwe_encrypt_noise(out + (size_t)c * (P->n + 1), gaussian32(mu[c], P->lwe_alpha), lwe_key, P->n);
     return TFHE_GPU_OK;
 }
 

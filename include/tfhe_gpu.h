@@ -100,14 +100,18 @@ size_t tfhe_gpu_tgsw_fft_bytes(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form);
 /* Device bytes the context holds (keys, tables, scratch). */
 size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
 
-/* Launch shape of the blind-rotation kernel of `form`: ciphertexts per CTA
- * (64 threads each).  split-FP32: 0 = automatic (6 when the batch fills
- * every SM six times over, else as few per CTA as spreads the batch over all
- * SMs); 1, 2, 4 = key rows read from L2 by every ciphertext; 5 = key rows
- * streamed once per CTA into a shared-memory ring by a producer warp; 6 = the
- * same ring fed by one consumer thread in line.  FP64: 3 (L2) or 4 (ring,
- * in line).  Engine tuning knob,
- * no counterpart in the reference (its kernel is a single HLS work-item). */
+/* Launch shape of the blind-rotation kernel of `form`.  split-FP32:
+ *   0 = automatic: whole waves of 6 ciphertexts per SM on the shared-ring
+ *       kernel, a remainder of at most 3 per SM on the pair kernel;
+ *   1, 2, 4 = ciphertexts (64 threads each) per CTA, key rows read from L2
+ *       by every ciphertext;
+ *   5 = 5 per CTA, key rows streamed once per CTA into a shared-memory ring
+ *       by a producer warp;
+ *   6, 7, 8 = that many per CTA, the same ring fed by one consumer thread;
+ *   11, 12, 13 = pair kernel: two 64-thread halves per ciphertext (about
+ *       half the latency), 1, 2, 3 ciphertexts per CTA, shared ring.
+ * FP64: 3 (L2) or 4 (ring, in line).  Engine tuning knob, no counterpart in
+ * the reference (its kernel is a single HLS work-item). */
 tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,
                                             int32_t groups);
 int32_t tfhe_gpu_get_groups_per_cta(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form);
@@ -130,6 +134,25 @@ tfhe_gpu_status tfhe_gpu_upload_bootstrapping_key_fft(tfhe_gpu_ctx* ctx,
 /* Upload the key-switching key (host int32 [kN][t][base][n+1]),
  * lwe-keyswitch-functions.cpp:85-99, 163-215. */
 tfhe_gpu_status tfhe_gpu_upload_keyswitch_key(tfhe_gpu_ctx* ctx, const int32_t* ks);
+
+/* Both cloud keys at once: the bootstrapping key (time domain, as
+ * tfhe_gpu_upload_bootstrapping_key) and the key-switching key (as
+ * tfhe_gpu_upload_keyswitch_key).  The upstream cloud keyset the test bench
+ * loads (test_bench/server/cloud.c:42-44) carries exactly these two. */
+tfhe_gpu_status tfhe_gpu_upload_cloud_key(tfhe_gpu_ctx* ctx, const int32_t* bk,
+                                          const int32_t* ks, uint32_t form_mask);
+
+/* Key generation for this context, with the bootstrapping key's arithmetic
+ * on the GPU: the LWE key, TLWE key, key-switching key and every random
+ * value of the bootstrapping key are drawn on the host in the order of
+ * tfhe_client_gate_keyset (same generator state, bit-identical keys); the n
+ * (k+1) l products a * s and the gadget terms are computed on the device,
+ * and the key goes straight into the forms of form_mask together with the
+ * key-switching key.  bk may be NULL; else it receives the time-domain key
+ * (for export).  Upstream new_random_gate_bootstrapping_secret_keyset
+ * (test_bench/client/alice.c:17) plus the key upload. */
+tfhe_gpu_status tfhe_gpu_gate_keyset(tfhe_gpu_ctx* ctx, int32_t* lwe_key, int32_t* tlwe_key,
+                                     int32_t* ks, int32_t* bk, uint32_t form_mask);
 
 /* TGSW samples (device, count x TGSW int32) -> engine transform layout
  * (device, count x tfhe_gpu_tgsw_fft_bytes). Upstream tGswToFftConvert. */
@@ -197,6 +220,17 @@ tfhe_gpu_status tfhe_gpu_tfhe_bootstrap_woKS_FFT(tfhe_gpu_ctx* ctx, int32_t* out
                                                  const int32_t* x, int32_t mu,
                                                  int32_t count, tfhe_gpu_form form,
                                                  void* stream);
+/* Programmable bootstrap: the constant test vector mu of the gate bootstrap
+ * (tfhe_bootstrap_woKS_FFT.cpp:63-66) replaced by a polynomial tv (device,
+ * N int32; tv_stride = 0 shares one vector, N gives item c its own at
+ * tv + c N).  The output encrypts F(phase) where F(j) = tv[j] for
+ * j = round(2N phase) < N and -tv[j - N] above (negacyclic), i.e. a lookup
+ * table on the phase (tfhe_client_test_vector builds tv from a table).
+ * keyswitch = 1: out is count x (n+1) after the key switch; 0: count x
+ * (kN+1) extracted samples.  Device batch. */
+tfhe_gpu_status tfhe_gpu_bootstrap_tv(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* x,
+                                      const int32_t* tv, int32_t tv_stride, int32_t count,
+                                      tfhe_gpu_form form, int32_t keyswitch, void* stream);
 /* Full bootstrap LWE(n) -> LWE(n) (upstream tfhe_bootstrap_FFT). */
 tfhe_gpu_status tfhe_gpu_tfhe_bootstrap_FFT(tfhe_gpu_ctx* ctx, int32_t* out,
                                             const int32_t* x, int32_t mu, int32_t count,
@@ -224,6 +258,10 @@ tfhe_gpu_status tfhe_gpu_bootsGates_host(tfhe_gpu_ctx* ctx, const int32_t* gates
                                          int32_t uniform_gate, int32_t* out,
                                          const int32_t* ca, const int32_t* cb,
                                          int32_t count, tfhe_gpu_form form);
+/* Host-buffer form of tfhe_gpu_bootsMUX. */
+tfhe_gpu_status tfhe_gpu_bootsMUX_host(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* a,
+                                       const int32_t* b, const int32_t* c, int32_t count,
+                                       tfhe_gpu_form form);
 
 /* Same result as tfhe_gpu_bootsGates, but the call allocates no memory: its
  * intermediate samples live in a fixed 3.4 MB device array built into the
@@ -239,6 +277,31 @@ tfhe_gpu_status tfhe_gpu_bootsGates_noalloc(tfhe_gpu_ctx* ctx, const int32_t* ga
                                             int32_t* out, const int32_t* ca,
                                             const int32_t* cb, int32_t count,
                                             tfhe_gpu_form form, void* stream);
+
+/* ---- CUDA graph of a gate batch; launch-shape autotuner ----------------- */
+/* Capture the whole gate pipeline of one batch (combination, blind rotation
+ * and extraction, key switch) over fixed device buffers into a CUDA graph,
+ * replayed by tfhe_gpu_graph_launch with one submission.  The graph owns its
+ * intermediate buffers; the caller's buffers and the context's keys must
+ * outlive it (re-uploading a key frees the old one: rebuild the graph after
+ * that).  Creation runs the batch once eagerly.  No counterpart in the
+ * reference (the FPGA kernel is enqueued per call). */
+typedef struct tfhe_gpu_graph tfhe_gpu_graph;
+tfhe_gpu_status tfhe_gpu_graph_gates_create(tfhe_gpu_ctx* ctx, const int32_t* gates,
+                                            int32_t uniform_gate, int32_t* out,
+                                            const int32_t* ca, const int32_t* cb,
+                                            int32_t count, tfhe_gpu_form form,
+                                            tfhe_gpu_graph** graph);
+tfhe_gpu_status tfhe_gpu_graph_launch(tfhe_gpu_graph* graph, void* stream);
+/* Kernel nodes of the graph (the engine kernels one launch runs). */
+int32_t tfhe_gpu_graph_kernel_count(const tfhe_gpu_graph* graph);
+void tfhe_gpu_graph_destroy(tfhe_gpu_graph* graph);
+
+/* Time the blind-rotation launch shapes of `form` (tfhe_gpu_set_groups_per_cta)
+ * on `count` synthetic ciphertexts with CUDA events, keep the fastest as the
+ * context's shape and return it with its time. */
+tfhe_gpu_status tfhe_gpu_autotune(tfhe_gpu_ctx* ctx, tfhe_gpu_form form, int32_t count,
+                                  int32_t* best_shape, float* best_ms);
 
 /* ---- serving: continuous-batching gate server (test_bench/server/cloud.c) */
 /* The test_bench server runs one client's circuit gate by gate
@@ -289,6 +352,15 @@ tfhe_gpu_status tfhe_client_gate_keyset(const tfhe_params* params, int32_t* lwe_
 tfhe_gpu_status tfhe_client_encrypt_bits(const tfhe_params* params, const int32_t* bits,
                                          int32_t count, const int32_t* lwe_key,
                                          int32_t* out);
+/* Encrypt arbitrary Torus32 messages mu[count] (lweSymEncrypt,
+ * lwe-functions.cpp:40-53), e.g. modSwitchToTorus32(m, 2p) for the padded
+ * messages of a programmable bootstrap. */
+tfhe_gpu_status tfhe_client_encrypt_phases(const tfhe_params* params, const int32_t* mu,
+                                           int32_t count, const int32_t* lwe_key, int32_t* out);
+/* Test vector of a lookup table on p messages with a padding bit (message m
+ * encrypted at phase m/(2p)): tv[j] = table[m] over m's window, -table[0]
+ * over the top half-window (negacyclic wrap onto message 0). */
+tfhe_gpu_status tfhe_client_test_vector(int32_t N, const int32_t* table, int32_t p, int32_t* tv);
 /* bootsSymDecrypt: bit = phase > 0. */
 tfhe_gpu_status tfhe_client_decrypt_bits(const tfhe_params* params, const int32_t* samples,
                                          int32_t count, const int32_t* lwe_key,

@@ -286,6 +286,23 @@ class Oracle:
                                _p(np.ascontiguousarray(c, np.int32), I32P), _p(out, I32P))
         return out
 
+    def test_vector(self, N, table):
+        table = np.ascontiguousarray(table, np.int32)
+        tv = np.zeros(N, np.int32)
+        self.lib.orc_test_vector(N, _p(table, I32P), len(table), _p(tv, I32P))
+        return tv
+
+    def bootstrap_tv_batch(self, P, bk_fft, ks, tv, x, threads=0):
+        """Programmable bootstrap + key switch of the samples x (count x
+        (n+1)); tv is one vector (N) or one per sample (count x N)."""
+        x = np.ascontiguousarray(x, np.int32).reshape(-1, P.n + 1)
+        tv = np.ascontiguousarray(tv, np.int32)
+        stride = P.N if tv.ndim == 2 else 0
+        out = np.zeros_like(x)
+        self.lib.orc_bootstrap_tv_batch(ctypes.byref(P), _p(bk_fft, F64P), _p(ks, I32P), _p(tv, I32P),
+                                        stride, _p(x, I32P), _p(out, I32P), len(x), int(threads))
+        return out
+
     def boots_gate_batch(self, P, bk_fft, ks, gates, ca, cb, threads=0):
         gates = np.ascontiguousarray(gates, np.int32)
         ca = np.ascontiguousarray(ca, np.int32)

@@ -622,6 +622,45 @@ void orc_bootstrap_prologue(const orc_params* P, int32_t mu, const int32_t* x,
         std::memcpy(accum + k * N, testvect.data(), sizeof(int32_t) * N);
 }
 
+/* Programmable bootstrap (published TFHE algorithm, Chillotti, Joye,
+ * Paillier, "Programmable bootstrapping enables efficient homomorphic
+ * inference of deep neural networks", 2021): the constant test vector of
+ * tfhe_bootstrap_woKS_FFT.cpp:63-66 replaced by an arbitrary polynomial tv;
+ * acc = (0, X^{-barb} tv), blind rotation, extraction, key switch. */
+void orc_bootstrap_tv(const orc_params* P, const double* bk_fft, const int32_t* ks,
+                      const int32_t* tv, const int32_t* x, int32_t* out) {
+    const int32_t n = P->n, N = P->N, k = P->k, Nx2 = 2 * N;
+    std::vector<int32_t> bara(n), acc((size_t)(k + 1) * N, 0), u((size_t)k * N + 1);
+    const int32_t barb = orc_mod_switch_from_torus32(x[n], Nx2);
+    for (int32_t i = 0; i < n; i++) bara[i] = orc_mod_switch_from_torus32(x[i], Nx2);
+    orc_mul_by_xai(N, (Nx2 - barb) % Nx2, tv, acc.data() + (size_t)k * N);
+    orc_blind_rotate_fft(P, acc.data(), bk_fft, bara.data());
+    orc_extract(P, acc.data(), u.data());
+    orc_keyswitch(P, ks, u.data(), out);
+}
+
+void orc_bootstrap_tv_batch(const orc_params* P, const double* bk_fft, const int32_t* ks,
+                            const int32_t* tv, int32_t tv_stride, const int32_t* x,
+                            int32_t* out, int32_t count, int32_t threads) {
+    const int32_t w = P->n + 1;
+#pragma omp parallel for schedule(dynamic) num_threads(threads > 0 ? threads : omp_get_max_threads())
+    for (int32_t c = 0; c < count; ++c)
+        orc_bootstrap_tv(P, bk_fft, ks, tv + (size_t)c * tv_stride, x + (size_t)c * w,
+                         out + (size_t)c * w);
+}
+
+/* Test vector of a lookup table on p messages encoded with a padding bit
+ * (message m at phase m / (2p)): coefficient j is table[m_j] for the
+ * message m_j = floor((j p + N/2) / N) whose window holds j, and -table[0]
+ * for the top half-window (j >= N - N/(2p)), which the negacyclic wrap maps
+ * back onto message 0 for phases just below 0. */
+void orc_test_vector(int32_t N, const int32_t* table, int32_t p, int32_t* tv) {
+    for (int32_t j = 0; j < N; ++j) {
+        const int64_t m = ((int64_t)j * p + N / 2) / N;
+        tv[j] = m < p ? table[m] : (int32_t)(0u - (uint32_t)table[0]);
+    }
+}
+
 void orc_bootstrap_woks(const orc_params* P, const double* bk_fft, int32_t mu,
                         const int32_t* x, int32_t* out, int32_t exact,
                         const int32_t* bk) {

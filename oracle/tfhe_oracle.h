@@ -119,6 +119,17 @@ void orc_bootstrap_woks(const orc_params* P, const double* bk_fft, int32_t mu,
                         const int32_t* x, int32_t* out, int32_t exact,
                         const int32_t* bk);
 
+/* Programmable bootstrap: test vector tv (N int32) instead of the constant
+ * mu; with key switch.  _batch: count items, tv_stride int32 apart (0 = one
+ * shared vector), on `threads` OpenMP threads. */
+void orc_bootstrap_tv(const orc_params* P, const double* bk_fft, const int32_t* ks,
+                      const int32_t* tv, const int32_t* x, int32_t* out);
+void orc_bootstrap_tv_batch(const orc_params* P, const double* bk_fft, const int32_t* ks,
+                            const int32_t* tv, int32_t tv_stride, const int32_t* x,
+                            int32_t* out, int32_t count, int32_t threads);
+/* test vector of a lookup table on p padded messages (m at phase m/(2p)) */
+void orc_test_vector(int32_t N, const int32_t* table, int32_t p, int32_t* tv);
+
 /* Gate identifiers (shared with the engine's public header). */
 enum {
     ORC_GATE_NAND = 0, ORC_GATE_AND = 1, ORC_GATE_OR = 2, ORC_GATE_XOR = 3,

@@ -24,8 +24,21 @@ def declared_functions():
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", text):
             name = m.group(1)
-            if name.startswith(("tfhe_gpu_", "tfhe_client_")) and name not in ("tfhe_gpu_status",):
+            if name.startswith(("tfhe_gpu_", "tfhe_client_", "tfhe_keyfile_")) and name not in ("tfhe_gpu_status",):
                 names.add(name)
+    return sorted(names)
+
+
+def compat_functions():
+    """Functions declared by the upstream-API headers include/tfhe/*.h."""
+    names = set()
+    inc = os.path.join(ROOT, "include", "tfhe")
+    for f in sorted(os.listdir(inc)):
+        text = re.sub(r"/\*.*?\*/", "", open(os.path.join(inc, f)).read(), flags=re.S)
+        text = re.sub(r"typedef[^;]*;", "", text)
+        for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", text):
+            if m.group(1) not in ("defined",):
+                names.add(m.group(1))
     return sorted(names)
 
 
@@ -44,6 +57,17 @@ def test_library_exports_every_declared_symbol(pkg):
     assert not missing, missing
     # and the binding knows a signature for each of them
     assert set(declared_functions()) <= set(pkg.SIGNATURES)
+
+
+def test_library_exports_upstream_api(pkg):
+    names = compat_functions()
+    for must in ("bootsNAND", "bootsOR", "bootsAND", "bootsXOR", "bootsXNOR", "bootsMUX", "bootsCONSTANT",
+                 "new_tfheGateBootstrappingCloudKeySet_fromFile", "import_gate_bootstrapping_ciphertext_fromFile",
+                 "new_random_gate_bootstrapping_secret_keyset", "bootsSymEncrypt", "bootsSymDecrypt"):
+        assert must in names
+    lib = pkg.lib()
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
 
 
 def test_client_keygen_matches_oracle(pkg, oracle, keys):
@@ -117,3 +141,22 @@ def test_no_cpu_fallback_when_library_missing(pkg, tmp_path, monkeypatch):
     monkeypatch.setattr(pkg, "_LIB", None)
     with pytest.raises(ImportError):
         pkg.lib()
+
+
+def test_client_test_vector_and_oracle_lookup_table(pkg, oracle, keys):
+    """The host test-vector builder equals the oracle's, and the oracle's
+    programmable bootstrap with it evaluates the table on padded messages."""
+    P = pkg.default_params()
+    OP = pyoracle.default_params()
+    p = 8
+    f = (5 * np.arange(p) + 2) % p
+    table = np.array([pkg.mod_switch_to_torus32(int(v), 2 * p) for v in f], np.int32)
+    tv = pkg.test_vector(P.N, table)
+    assert (tv == oracle.test_vector(P.N, table)).all()
+    assert tv[0] == table[0] and tv[P.N - 1] == -table[0] and tv[P.N // 2] == table[p // 2]
+    m = np.arange(p)
+    pkg.set_seed([94])
+    x = pkg.encrypt_phases(P, [pkg.mod_switch_to_torus32(int(v), 2 * p) for v in m], keys["lwe"])
+    out = oracle.bootstrap_tv_batch(OP, keys["bk_fft"], keys["ks"], tv, x)
+    ph = pkg.phases(out, keys["lwe"]).astype(np.int64) & 0xFFFFFFFF
+    assert (((ph * 2 * p + (1 << 31)) >> 32) % (2 * p) == f[m]).all()

@@ -227,6 +227,8 @@ def test_errors_are_status_codes(pkg, keys, torch_cuda, P):
 
 @pytest.mark.parametrize("form,groups", [("split_fp32", 0), ("split_fp32", 1), ("split_fp32", 2),
                                          ("split_fp32", 4), ("split_fp32", 5), ("split_fp32", 6),
+                                         ("split_fp32", 7), ("split_fp32", 8),
+                                         ("split_fp32", 11), ("split_fp32", 12), ("split_fp32", 13),
                                          ("fp64", 3), ("fp64", 4)])
 def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, groups):
     """Each blind-rotation launch shape (L2-direct and shared-ring kernels) on
@@ -255,3 +257,65 @@ def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, grou
     ref = oracle.boots_gate_batch(P, keys["bk_fft"], keys["ks"], gates[:4], ca[:4], cb[:4])
     d = wrap_diff(oracle.phases(got[:4], keys["lwe"], P.n), oracle.phases(ref, keys["lwe"], P.n))
     assert np.abs(d).max() <= PHASE_TOL
+
+
+def test_auto_shape_full_wave_and_tail(pkg, oracle, keys, torch_cuda, P, inputs):
+    """The automatic split-FP32 shape on one full wave (6 per SM on the ring
+    kernel) plus a tail of 40 on the pair kernel: every output decrypts to the
+    truth and ciphertexts from both launches match the oracle's phases."""
+    torch = torch_cuda
+    a, b, ca, cb = inputs
+    count = 6 * 152 + 40
+    reps = (count + len(a) - 1) // len(a)
+    a, b = np.tile(a, reps)[:count], np.tile(b, reps)[:count]
+    ca, cb = np.tile(ca, (reps, 1))[:count], np.tile(cb, (reps, 1))[:count]
+    e = pkg.Engine(pkg.default_params())
+    try:
+        e.upload_bootstrapping_key(keys["bk"], forms=("split_fp32",))
+        e.upload_keyswitch_key(keys["ks"])
+        assert e.get_groups_per_cta("split_fp32") == 0
+        gates = (np.arange(count, dtype=np.int32) * 7) % 10
+        d_out = torch.zeros((count, P.n + 1), dtype=torch.int32, device="cuda")
+        e.bootsGates(dev(torch, gates), d_out, dev(torch, ca), dev(torch, cb), count, "split_fp32",
+                     stream=cur(torch))
+        torch.cuda.synchronize()
+        e.synchronize()
+        got = host(d_out)
+    finally:
+        e.close()
+    names = sorted(pyoracle.GATES, key=lambda g: pyoracle.GATES[g])
+    truth = np.array([pyoracle.GATE_FN[names[g]](x, y) for g, x, y in zip(gates, a, b)])
+    assert (oracle.decrypt_bits(P, got, keys["lwe"]) == truth).all()
+    idx = np.array([0, 1, 911, 912, 913, count - 1])
+    ref = oracle.boots_gate_batch(P, keys["bk_fft"], keys["ks"], gates[idx], ca[idx], cb[idx])
+    d = wrap_diff(oracle.phases(got[idx], keys["lwe"], P.n), oracle.phases(ref, keys["lwe"], P.n))
+    assert np.abs(d).max() <= PHASE_TOL
+
+
+@pytest.mark.parametrize("params", ["default", "stress"])
+def test_gpu_keyset_is_the_host_keyset(pkg, oracle, torch_cuda, params):
+    """tfhe_gpu_gate_keyset (random values on the host, products on the GPU)
+    gives the same keys bit for bit as the host keygen from the same seed,
+    and the keys it uploaded bootstrap correctly."""
+    P = pkg.default_params() if params == "default" else pkg.stress_params()
+    want = pkg.gate_keyset(P, [31, 41])
+    e = pkg.Engine(P)
+    try:
+        got = e.gate_keyset([31, 41])
+        for a, b in zip(got, want):
+            assert (a == b).all()
+        torch = torch_cuda
+        rng = np.random.default_rng(95)
+        bits = rng.integers(0, 2, (2, 16))
+        pkg.set_seed([95])
+        ca = pkg.encrypt_bits(P, bits[0], got[0])
+        cb = pkg.encrypt_bits(P, bits[1], got[0])
+        d_out = torch.zeros((16, P.n + 1), dtype=torch.int32, device="cuda")
+        for form in ("split_fp32", "fp64"):
+            e.bootsGate("NAND", d_out, torch.from_numpy(ca).cuda(), torch.from_numpy(cb).cuda(), 16, form,
+                        stream=torch.cuda.current_stream().cuda_stream)
+            torch.cuda.synchronize()
+            e.synchronize()
+            assert (pkg.decrypt_bits(P, d_out.cpu().numpy(), got[0]) == 1 - (bits[0] & bits[1])).all()
+    finally:
+        e.close()
