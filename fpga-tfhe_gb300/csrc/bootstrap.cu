@@ -110,6 +110,20 @@ __device__ __forceinline__ uint32_t round_wrap_u32(float v) {
     return ((uint32_t)i1 << 16) + (uint32_t)i2;
 }
 
+// Gadget digit of u at `decal` as a transform input: ((u >> decal) & mask) -
+// halfBg.  FP32: the masked digit m < 2^22 ORed into the encoding of the
+// magic constant is the float M + m, and one subtraction of M + halfBg
+// gives m - halfBg exactly.
+template <typename R>
+__device__ __forceinline__ R digit_value(uint32_t u, int decal, uint32_t mask, int halfBg) {
+    if constexpr (sizeof(R) == 4) {
+        return __int_as_float((int32_t)(((u >> decal) & mask) | (uint32_t)kRoundMagicBits)) -
+               (kRoundMagic + (float)halfBg);
+    } else {
+        return (R)((int)((u >> decal) & mask) - halfBg);
+    }
+}
+
 template <typename R>
 __device__ __forceinline__ int64_t to_int(R v);
 template <>
@@ -349,6 +363,133 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
             } else {
                 dst[x0] = (int32_t)c0[q];
                 dst[x0 + kHalf] = (int32_t)c1[q];
+            }
+        }
+    }
+    group_sync(S.bar_id);
+}
+
+// Rounding of one transformed-back polynomial part into c0/c1 (the 16
+// coefficients x0 = t + 64q and x0 + 512 of this thread): FP32 parts --
+// the high part (pt = 0) rounded and shifted by the split, the low part
+// (pt = 1) added; FP64 -- the reference's truncating conversion.
+template <typename R, int PARTS>
+__device__ __forceinline__ void round_part(const cpx<R> (&v)[8], int pt, int split, uint32_t (&c0)[8],
+                                           uint32_t (&c1)[8]) {
+    if constexpr (sizeof(R) == 4) {
+        if (PARTS == 2 && pt == 0) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                c0[q] = round_small_u32(v[q].x) << split;
+                c1[q] = round_small_u32(v[q].y) << split;
+            }
+        } else if (PARTS == 2) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                c0[q] += round_wrap_u32(v[q].x);
+                c1[q] += round_wrap_u32(v[q].y);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                c0[q] = round_wrap_u32(v[q].x);
+                c1[q] = round_wrap_u32(v[q].y);
+            }
+        }
+    } else {
+        const R inv = (R)(1.0 / 512.0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            c0[q] = (uint32_t)(uint64_t)to_int<R>(v[q].x * inv);
+            c1[q] = (uint32_t)(uint64_t)to_int<R>(v[q].y * inv);
+        }
+    }
+}
+
+// out[j][pt] into v, (j, pt) uniform at run time, indices compile-time so
+// that out stays in registers.
+template <typename R, int PARTS>
+__device__ __forceinline__ void pick_part(cpx<R> (&v)[8], const cpx<R> (&out)[2][PARTS][8], int j, int pt) {
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+        for (int pp = 0; pp < PARTS; ++pp)
+            if (jj == j && pp == pt) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) v[q] = out[jj][pp][q];
+            }
+}
+
+// out[j][pt] += w, (j, pt) uniform at run time.
+template <typename R, int PARTS>
+__device__ __forceinline__ void add_part(cpx<R> (&out)[2][PARTS][8], const cpx<R> (&w)[8], int j, int pt) {
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+        for (int pp = 0; pp < PARTS; ++pp)
+            if (jj == j && pp == pt) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) out[jj][pp][q] = cadd(out[jj][pp][q], w[q]);
+            }
+}
+
+// The fused step of the shared-ring kernel, with one copy of each transform
+// in the code: the levels and the (output, part) pairs are run-time loops
+// (a fully unrolled step overflows the instruction cache).
+template <typename R, int PARTS, int L, typename Keys>
+__device__ __forceinline__ void ep_step_lean(const StepCtx<R, PARTS, 1>& S, Keys& keys, int a) {
+    const int t = S.t;
+    const int halfBg = 1 << (S.Bgbit - 1);
+    const uint32_t mask = (1u << S.Bgbit) - 1;
+
+    cpx<R> out[2][PARTS][8];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int pt = 0; pt < PARTS; ++pt)
+#pragma unroll
+            for (int q = 0; q < 8; ++q) out[j][pt][q] = {(R)0, (R)0};
+
+#pragma unroll 1
+    for (int jp = 0; jp < 2; ++jp) {
+        const int32_t* src = S.acc + jp * kN;
+        uint32_t r0[8], r1[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int x0 = t + 64 * r;
+            r0[r] = (uint32_t)rot_coef(src, x0, a) - (uint32_t)src[x0] + S.offset;
+            r1[r] = (uint32_t)rot_coef(src, x0 + kHalf, a) - (uint32_t)src[x0 + kHalf] + S.offset;
+        }
+#pragma unroll 1
+        for (int lev = 0; lev < L; ++lev) {
+            const int decal = 32 - (lev + 1) * S.Bgbit;
+            cpx<R> v[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                v[r] = cpx<R>{digit_value<R>(r0[r], decal, mask, halfBg),
+                              digit_value<R>(r1[r], decal, mask, halfBg)};
+            fft512_forward_tw(v, S.s[0], S.tw, t, S.bar_id);
+            const int p = jp * L + lev;
+            mac_row<R, PARTS, Keys::kShared>(out, v, keys.acquire(p), t);
+            keys.release(p);
+        }
+    }
+
+    uint32_t c0[8], c1[8];
+#pragma unroll 1
+    for (int u = 0; u < 2 * PARTS; ++u) {
+        const int j = u / PARTS, pt = u % PARTS;
+        cpx<R> v[8];
+        pick_part<R, PARTS>(v, out, j, pt);
+        fft512_inverse_tw(v, S.s[0], S.tw, t, S.bar_id);
+        round_part<R, PARTS>(v, pt, S.split, c0, c1);
+        if (pt == PARTS - 1) {
+            int32_t* dst = S.acc + j * kN;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int x0 = t + 64 * q;
+                dst[x0] = (int32_t)((uint32_t)dst[x0] + c0[q]);
+                dst[x0 + kHalf] = (int32_t)((uint32_t)dst[x0 + kHalf] + c1[q]);
             }
         }
     }
@@ -640,7 +781,7 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
             }
             continue;
         }
-        ep_step<R, PARTS, true, L, 1, 1, 1>(St, keys, ai);
+        ep_step_lean<R, PARTS, L>(St, keys, ai);
     }
     if (keys.producer) keys.drain();
     if (a.acc_out) {
@@ -674,12 +815,11 @@ __device__ __forceinline__ void pair_sync(int bar_id) {
     asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(2 * kFftThreads) : "memory");
 }
 
-// H is the half (a compile-time constant so that out[H] and out[1 - H] stay
-// in registers).
-template <typename R, int PARTS, int L, int H, typename Keys>
-__device__ __forceinline__ void ep_step_half(const StepCtx<R, PARTS, 1>& S, Keys& keys, int a,
+// h is the half; out[h] and out[1 - h] are picked by uniform branches so
+// that the accumulators stay in registers with one copy of the code.
+template <typename R, int PARTS, int L, typename Keys>
+__device__ __forceinline__ void ep_step_half(const StepCtx<R, PARTS, 1>& S, Keys& keys, int a, int h,
                                              cpx<R>* peer_inbox, int pair_bar) {
-    constexpr int h = H;
     const int t = S.t;
     const int halfBg = 1 << (S.Bgbit - 1);
     const uint32_t mask = (1u << S.Bgbit) - 1;
@@ -701,16 +841,14 @@ __device__ __forceinline__ void ep_step_half(const StepCtx<R, PARTS, 1>& S, Keys
             r0[r] = (uint32_t)rot_coef(src, x0, a) - (uint32_t)src[x0] + S.offset;
             r1[r] = (uint32_t)rot_coef(src, x0 + kHalf, a) - (uint32_t)src[x0 + kHalf] + S.offset;
         }
-#pragma unroll
+#pragma unroll 1
         for (int lev = 0; lev < L; ++lev) {
             cpx<R> v[8];
             const int decal = 32 - (lev + 1) * S.Bgbit;
 #pragma unroll
-            for (int r = 0; r < 8; ++r) {
-                const int d0 = (int)((r0[r] >> decal) & mask) - halfBg;
-                const int d1 = (int)((r1[r] >> decal) & mask) - halfBg;
-                v[r] = cpx<R>{(R)d0, (R)d1};
-            }
+            for (int r = 0; r < 8; ++r)
+                v[r] = cpx<R>{digit_value<R>(r0[r], decal, mask, halfBg),
+                              digit_value<R>(r1[r], decal, mask, halfBg)};
             fft512_forward_tw(v, S.s[0], S.tw, t, S.bar_id);
             const int p = h * L + lev;
             mac_row<R, PARTS, Keys::kShared>(out, v, keys.acquire(p), t);
@@ -725,57 +863,34 @@ __device__ __forceinline__ void ep_step_half(const StepCtx<R, PARTS, 1>& S, Keys
     // half's scratch, then read this half's own
     pair_sync(pair_bar);
 #pragma unroll
-    for (int pt = 0; pt < PARTS; ++pt)
+    for (int pt = 0; pt < PARTS; ++pt) {
+        cpx<R> w[8];
+        pick_part<R, PARTS>(w, out, 1 - h, pt);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) peer_inbox[pt * kScratchStride + q * 64 + t] = out[1 - h][pt][q];
+        for (int q = 0; q < 8; ++q) peer_inbox[pt * kScratchStride + q * 64 + t] = w[q];
+    }
     pair_sync(pair_bar);
     // the next step's first rows land during this step's inverse transforms
     if (keys.producer) keys.issue_upto(keys.row0 + 2 * L - 1);
     {
         const cpx<R>* inbox = S.s[0].b0;
 #pragma unroll
-        for (int pt = 0; pt < PARTS; ++pt)
+        for (int pt = 0; pt < PARTS; ++pt) {
+            cpx<R> w[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q)
-                out[h][pt][q] = cadd(out[h][pt][q], inbox[pt * kScratchStride + q * 64 + t]);
+            for (int q = 0; q < 8; ++q) w[q] = inbox[pt * kScratchStride + q * 64 + t];
+            add_part<R, PARTS>(out, w, h, pt);
+        }
     }
     group_sync(S.bar_id);  // the inbox is the transform's scratch
 
-    const R inv = (R)(1.0 / 512.0);
     uint32_t c0[8], c1[8];
-#pragma unroll
+#pragma unroll 1
     for (int pt = 0; pt < PARTS; ++pt) {
         cpx<R> v[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = out[h][pt][q];
+        pick_part<R, PARTS>(v, out, h, pt);
         fft512_inverse_tw(v, S.s[0], S.tw, t, S.bar_id);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const cpx<R> z = v[q];
-            uint32_t a0, a1;
-            if constexpr (sizeof(R) == 4) {
-                if (PARTS == 2 && pt == 0) {
-                    a0 = round_small_u32(z.x);
-                    a1 = round_small_u32(z.y);
-                } else {
-                    a0 = round_wrap_u32(z.x);
-                    a1 = round_wrap_u32(z.y);
-                }
-            } else {
-                a0 = (uint32_t)(uint64_t)to_int<R>(z.x * inv);
-                a1 = (uint32_t)(uint64_t)to_int<R>(z.y * inv);
-            }
-            if (PARTS == 1) {
-                c0[q] = a0;
-                c1[q] = a1;
-            } else if (pt == 0) {
-                c0[q] = a0 << S.split;
-                c1[q] = a1 << S.split;
-            } else {
-                c0[q] += a0;
-                c1[q] += a1;
-            }
-        }
+        round_part<R, PARTS>(v, pt, S.split, c0, c1);
     }
     int32_t* dst = S.acc + h * kN;
 #pragma unroll
@@ -874,8 +989,7 @@ __global__ void __launch_bounds__(128 * PAIRS, 1) k_blind_rotate_pair(KParams kp
             }
             continue;
         }
-        if (h == 0) ep_step_half<R, PARTS, L, 0>(St, keys, ai, peer_inbox, pair_bar);
-        else ep_step_half<R, PARTS, L, 1>(St, keys, ai, peer_inbox, pair_bar);
+        ep_step_half<R, PARTS, L>(St, keys, ai, h, peer_inbox, pair_bar);
     }
     if (keys.producer) {
         keys.issue_through(keys.total - 1);  // rows of a skipped last step
