@@ -85,6 +85,23 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(value, world, device):
+    """The maximum of a per-rank number over all ranks of the job (the job's
+    time is its slowest rank's); the value itself on one rank."""
+    if world <= 1:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, world, max_ms):
+    """Whole-job units per second: every rank processed units_per_rank
+    independent units (replicas), the job took the slowest rank's time."""
+    return world * units_per_rank / (max_ms / 1000.0)
+
+
 def make_inputs(pkg, P, lwe_key, batch, seed=4):
     rng = np.random.default_rng(seed)
     a = rng.integers(0, 2, batch)
@@ -632,12 +649,8 @@ def main():
     with ClockSampler(local) as clk:
         ms = timed(args.form, args.steps)
     torch.cuda.synchronize()
-    total_ms = sum(ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * batch * args.steps / (total_ms / 1000.0)
+    total_ms = max_over_ranks(sum(ms), world, dev)
+    value = job_throughput(batch * args.steps, world, total_ms)
     truth = {0: lambda x, y: 1 - (x & y), 1: lambda x, y: x & y, 2: lambda x, y: x | y,
              3: lambda x, y: x ^ y}
     d_out.zero_()
@@ -665,12 +678,8 @@ def main():
             raise RuntimeError("bootsGates_host failed: %d" % st)
         if s >= args.warmup:
             e2e_ms.append(1000 * (time.perf_counter() - t0))
-    e2e_total = sum(e2e_ms)
-    if world > 1:
-        t = torch.tensor([e2e_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * batch * args.steps / (e2e_total / 1000.0)
+    e2e_total = max_over_ranks(sum(e2e_ms), world, dev)
+    e2e_value = job_throughput(batch * args.steps, world, e2e_total)
     lwe_bytes = batch * (P.n + 1) * 4
 
     # dominant kernel alone: blind rotation + extraction on resident inputs
