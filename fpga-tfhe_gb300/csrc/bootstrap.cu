@@ -195,6 +195,7 @@ __device__ __forceinline__ FftTwiddles<R> hot_twiddles(const cpx<R>* hot) {
 template <typename R, int PARTS, int NB>
 struct StepCtx {
     FftTwiddles<R> tw;  // smem twiddles: a = psi^t W^(tq) (twist folded), b = W^(8jq)
+    FftIdx ix;          // this thread's exchange slots
     FftScratch<R> s[NB];
     int32_t* acc;       // smem 2 x N
     int t, bar_id;
@@ -296,7 +297,7 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
                     v[b][r] = cpx<R>{(R)d0, (R)d1};
                 }
             }
-            fft512_forward_tw_multi<FB>(v, *reinterpret_cast<const FftScratch<R>(*)[FB]>(S.s), S.tw, t,
+            fft512_forward_tw_multi<FB>(v, *reinterpret_cast<const FftScratch<R>(*)[FB]>(S.s), S.tw, S.ix, t,
                                         S.bar_id);
 #pragma unroll
             for (int b = 0; b < FB; ++b) {
@@ -319,7 +320,7 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
             for (int b = 0; b < IB; ++b)
 #pragma unroll
                 for (int q = 0; q < 8; ++q) v[b][q] = out[j][pt0 + b][q];
-            fft512_inverse_tw_multi<IB>(v, *reinterpret_cast<const FftScratch<R>(*)[IB]>(S.s), S.tw, t,
+            fft512_inverse_tw_multi<IB>(v, *reinterpret_cast<const FftScratch<R>(*)[IB]>(S.s), S.tw, S.ix, t,
                                         S.bar_id);
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
@@ -468,7 +469,7 @@ __device__ __forceinline__ void ep_step_lean(const StepCtx<R, PARTS, 1>& S, Keys
             for (int r = 0; r < 8; ++r)
                 v[r] = cpx<R>{digit_value<R>(r0[r], decal, mask, halfBg),
                               digit_value<R>(r1[r], decal, mask, halfBg)};
-            fft512_forward_tw(v, S.s[0], S.tw, t, S.bar_id);
+            fft512_forward_tw(v, S.s[0], S.tw, S.ix, t, S.bar_id);
             const int p = jp * L + lev;
             mac_row<R, PARTS, Keys::kShared>(out, v, keys.acquire(p), t);
             keys.release(p);
@@ -481,7 +482,7 @@ __device__ __forceinline__ void ep_step_lean(const StepCtx<R, PARTS, 1>& S, Keys
         const int j = u / PARTS, pt = u % PARTS;
         cpx<R> v[8];
         pick_part<R, PARTS>(v, out, j, pt);
-        fft512_inverse_tw(v, S.s[0], S.tw, t, S.bar_id);
+        fft512_inverse_tw(v, S.s[0], S.tw, S.ix, t, S.bar_id);
         round_part<R, PARTS>(v, pt, S.split, c0, c1);
         if (pt == PARTS - 1) {
             int32_t* dst = S.acc + j * kN;
@@ -519,6 +520,7 @@ __global__ void __launch_bounds__(64 * GROUPS, 1) k_external_product(KParams kp,
     char* gbase = smem + Plan::tables + (size_t)g * Plan::group;
     Ctx S;
     S.tw = hot_twiddles<R>(tables);
+    S.ix = make_fft_idx(t);
     S.acc = reinterpret_cast<int32_t*>(gbase);
 #pragma unroll
     for (int b = 0; b < NB; ++b)
@@ -746,6 +748,7 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
     char* gbase = smem + Plan::group_off + (size_t)g * Plan::group;
     StepCtx<R, PARTS, 1> St;
     St.tw = hot_twiddles<R>(tables);
+    St.ix = make_fft_idx(t);
     St.acc = reinterpret_cast<int32_t*>(gbase);
     St.s[0] = scratch_at<R>(gbase + Plan::acc);
     St.t = t;
@@ -849,7 +852,7 @@ __device__ __forceinline__ void ep_step_half(const StepCtx<R, PARTS, 1>& S, Keys
             for (int r = 0; r < 8; ++r)
                 v[r] = cpx<R>{digit_value<R>(r0[r], decal, mask, halfBg),
                               digit_value<R>(r1[r], decal, mask, halfBg)};
-            fft512_forward_tw(v, S.s[0], S.tw, t, S.bar_id);
+            fft512_forward_tw(v, S.s[0], S.tw, S.ix, t, S.bar_id);
             const int p = h * L + lev;
             mac_row<R, PARTS, Keys::kShared>(out, v, keys.acquire(p), t);
             keys.release(p);
@@ -889,7 +892,7 @@ __device__ __forceinline__ void ep_step_half(const StepCtx<R, PARTS, 1>& S, Keys
     for (int pt = 0; pt < PARTS; ++pt) {
         cpx<R> v[8];
         pick_part<R, PARTS>(v, out, h, pt);
-        fft512_inverse_tw(v, S.s[0], S.tw, t, S.bar_id);
+        fft512_inverse_tw(v, S.s[0], S.tw, S.ix, t, S.bar_id);
         round_part<R, PARTS>(v, pt, S.split, c0, c1);
     }
     int32_t* dst = S.acc + h * kN;
@@ -952,6 +955,7 @@ __global__ void __launch_bounds__(128 * PAIRS, 1) k_blind_rotate_pair(KParams kp
     char* pbase = smem + Plan::pair_off + (size_t)pr * Plan::pair;
     StepCtx<R, PARTS, 1> St;
     St.tw = hot_twiddles<R>(tables);
+    St.ix = make_fft_idx(t);
     St.acc = reinterpret_cast<int32_t*>(pbase);
     St.s[0] = scratch_at<R>(pbase + Plan::acc + h * Plan::half_scratch);
     cpx<R>* peer_inbox = reinterpret_cast<cpx<R>*>(pbase + Plan::acc + (1 - h) * Plan::half_scratch);

@@ -7,6 +7,7 @@
 // host instead exits the process on an OpenCL error (host.h:13-18).
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -44,12 +45,17 @@ cudaStream_t pick(tfhe_gpu_ctx* ctx, void* stream) {
 }
 
 int32_t auto_split_bits(const tfhe_params& P) {
-    // The high part Khi of the key (32 - s bits) must make the FP32 product
-    // sum_p D_p * Khi_p exact after rounding: its size grows with the digit
-    // size (Bgbit) and the number of terms (N (k+1) l).  s = 24 keeps it
-    // below ~2^19 for the default set; every extra digit bit moves s up one.
-    int s = 24 + (P.Bgbit - 7);
-    if (P.l * (P.k + 1) > 6) s += 1;
+    // The split K = Khi 2^s + Klo trades two FP32 errors: the high product
+    // sum_p D_p * Khi_p must round to exact integers (its size grows with the
+    // digits, sqrt((k+1) l N) terms and the 32 - s bits of Khi), while the
+    // low product's rounding error grows with 2^s.  Measured on the output
+    // phase noise (bench --workload failures / stress --split-bits): the
+    // optimum keeps the high product at the same size, s = floor(Bgbit +
+    // log2((k+1) l N) / 2 + 10.75): 24 for the default set (sigma 0.00337 /
+    // 0.00325 / 0.00330 / 0.00347 turn at s = 23..26) and 26 for n=500, l=2,
+    // Bgbit=10 (0.096 / 0.0263 / 0.0291 / 0.0387 at s = 25..28; FP64 0.0253).
+    const double terms = (double)(P.k + 1) * P.l * P.N;
+    int s = (int)std::floor(P.Bgbit + 0.5 * std::log2(terms) + 10.75);
     if (s < 16) s = 16;
     if (s > 30) s = 30;
     return s;

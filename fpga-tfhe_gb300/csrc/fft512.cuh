@@ -258,6 +258,46 @@ __device__ __forceinline__ void fft512_inverse_multi(cpx<R> (&v)[NB][8], const F
     }
 }
 
+// Per-thread exchange slots of the FP32 swizzle, in closed form for each
+// access pattern (computed once per thread; an access is then an immediate
+// offset or one XOR):
+//   A: slot(t + 64q)          = 64q + (q odd ? a1 : a0)
+//   B: slot(64(t/8) + t%8 + 8r) = b_base + 16(r/2) + (b_x ^ (8(r%2) | r/2))
+//   C: slot(8t + r)           = c_base + (r ^ c_z)
+// FP64 keeps the padded layout (slot<double>), computed per access.
+struct FftIdx {
+    int a0, a1, b_base, b_x, c_base, c_z;
+};
+
+__device__ __forceinline__ FftIdx make_fft_idx(int t) {
+    const int b = t >> 3, j = t & 7;
+    const int gC = ((t >> 1) & 7) | (((t >> 1) & 4) << 1);
+    FftIdx x;
+    x.a0 = t ^ (t >> 4);
+    x.a1 = t ^ ((t >> 4) | 12);
+    x.b_base = 64 * b;
+    x.b_x = j ^ (12 * (b & 1));
+    x.c_base = (8 * t) ^ (gC & 8);
+    x.c_z = gC & 7;
+    return x;
+}
+
+template <typename R>
+__device__ __forceinline__ int slot_a(const FftIdx& x, int t, int q) {
+    if constexpr (sizeof(R) == 4) return 64 * q + ((q & 1) ? x.a1 : x.a0);
+    else return slot<R>(t + 64 * q);
+}
+template <typename R>
+__device__ __forceinline__ int slot_b(const FftIdx& x, int t, int r) {
+    if constexpr (sizeof(R) == 4) return x.b_base + 16 * (r >> 1) + (x.b_x ^ ((8 * (r & 1)) | (r >> 1)));
+    else return slot<R>(64 * (t >> 3) + (t & 7) + 8 * r);
+}
+template <typename R>
+__device__ __forceinline__ int slot_c(const FftIdx& x, int t, int r) {
+    if constexpr (sizeof(R) == 4) return x.c_base + (r ^ x.c_z);
+    else return slot<R>(8 * t + r);
+}
+
 // ----------------------------------------------------------------------
 // Transforms with the negacyclic twist folded in.  Point x = t + 64r of a
 // thread is twisted by psi^x = psi^t c_r, c_r = psi^(64 r) = e^{i pi r/16}:
@@ -285,7 +325,8 @@ __device__ __forceinline__ cpx<R> twist_c(int r) {
 // of the transform of the twisted sequence.  tw.a = psi^t W^(tq) table.
 template <int NB, typename R>
 __device__ __forceinline__ void fft512_forward_tw_multi(cpx<R> (&v)[NB][8], const FftScratch<R> (&s)[NB],
-                                                        const FftTwiddles<R>& tw, int t, int bar_id) {
+                                                        const FftTwiddles<R>& tw, const FftIdx& ix, int t,
+                                                  int bar_id) {
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
@@ -294,25 +335,25 @@ __device__ __forceinline__ void fft512_forward_tw_multi(cpx<R> (&v)[NB][8], cons
 #pragma unroll
         for (int q = 0; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.a[q * 64 + t]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b0[slot<R>(t + 64 * q)] = v[b][q];
+        for (int q = 0; q < 8; ++q) s[b].b0[slot_a<R>(ix, t, q)] = v[b][q];
     }
     group_sync(bar_id);
     const int hb = t >> 3, j = t & 7;
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b0[slot<R>(64 * hb + j + 8 * r)];
+        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b0[slot_b<R>(ix, t, r)];
         dft8<1>(v[b]);
 #pragma unroll
         for (int q = 1; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.b[q * 8 + j]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b1[slot<R>(64 * hb + j + 8 * q)] = v[b][q];
+        for (int q = 0; q < 8; ++q) s[b].b1[slot_b<R>(ix, t, q)] = v[b][q];
     }
     group_sync(bar_id);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b1[slot<R>(8 * t + r)];
+        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b1[slot_c<R>(ix, t, r)];
         dft8<1>(v[b]);
     }
 }
@@ -321,12 +362,13 @@ __device__ __forceinline__ void fft512_forward_tw_multi(cpx<R> (&v)[NB][8], cons
 // psi^-(t + 64q)), not yet divided by 512.
 template <int NB, typename R>
 __device__ __forceinline__ void fft512_inverse_tw_multi(cpx<R> (&v)[NB][8], const FftScratch<R> (&s)[NB],
-                                                        const FftTwiddles<R>& tw, int t, int bar_id) {
+                                                        const FftTwiddles<R>& tw, const FftIdx& ix, int t,
+                                                  int bar_id) {
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
         dft8<-1>(v[b]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b0[slot<R>(8 * t + q)] = v[b][q];
+        for (int q = 0; q < 8; ++q) s[b].b0[slot_c<R>(ix, t, q)] = v[b][q];
     }
     group_sync(bar_id);
     const int hb = t >> 3, j = t & 7;
@@ -334,18 +376,18 @@ __device__ __forceinline__ void fft512_inverse_tw_multi(cpx<R> (&v)[NB][8], cons
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-            v[b][r] = s[b].b0[slot<R>(64 * hb + j + 8 * r)];
+            v[b][r] = s[b].b0[slot_b<R>(ix, t, r)];
             if (r) v[b][r] = cmulc(v[b][r], tw.b[r * 8 + j]);
         }
         dft8<-1>(v[b]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b1[slot<R>(64 * hb + j + 8 * q)] = v[b][q];
+        for (int q = 0; q < 8; ++q) s[b].b1[slot_b<R>(ix, t, q)] = v[b][q];
     }
     group_sync(bar_id);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) v[b][r] = cmulc(s[b].b1[slot<R>(t + 64 * r)], tw.a[r * 64 + t]);
+        for (int r = 0; r < 8; ++r) v[b][r] = cmulc(s[b].b1[slot_a<R>(ix, t, r)], tw.a[r * 64 + t]);
         dft8<-1>(v[b]);
 #pragma unroll
         for (int q = 1; q < 8; ++q) v[b][q] = cmulc(v[b][q], twist_c<R>(q));
@@ -354,16 +396,18 @@ __device__ __forceinline__ void fft512_inverse_tw_multi(cpx<R> (&v)[NB][8], cons
 
 template <typename R>
 __device__ __forceinline__ void fft512_forward_tw(cpx<R> (&v)[8], const FftScratch<R>& s,
-                                                  const FftTwiddles<R>& tw, int t, int bar_id) {
+                                                  const FftTwiddles<R>& tw, const FftIdx& ix, int t,
+                                                  int bar_id) {
     fft512_forward_tw_multi<1>(*reinterpret_cast<cpx<R>(*)[1][8]>(&v),
-                               *reinterpret_cast<const FftScratch<R>(*)[1]>(&s), tw, t, bar_id);
+                               *reinterpret_cast<const FftScratch<R>(*)[1]>(&s), tw, ix, t, bar_id);
 }
 
 template <typename R>
 __device__ __forceinline__ void fft512_inverse_tw(cpx<R> (&v)[8], const FftScratch<R>& s,
-                                                  const FftTwiddles<R>& tw, int t, int bar_id) {
+                                                  const FftTwiddles<R>& tw, const FftIdx& ix, int t,
+                                                  int bar_id) {
     fft512_inverse_tw_multi<1>(*reinterpret_cast<cpx<R>(*)[1][8]>(&v),
-                               *reinterpret_cast<const FftScratch<R>(*)[1]>(&s), tw, t, bar_id);
+                               *reinterpret_cast<const FftScratch<R>(*)[1]>(&s), tw, ix, t, bar_id);
 }
 
 // Frequency held at (thread t, register q) after the forward transform.

@@ -319,3 +319,46 @@ def test_gpu_keyset_is_the_host_keyset(pkg, oracle, torch_cuda, params):
             assert (pkg.decrypt_bits(P, d_out.cpu().numpy(), got[0]) == 1 - (bits[0] & bits[1])).all()
     finally:
         e.close()
+
+
+def test_stress_set_noise_band(pkg, torch_cuda):
+    """The alternative set (n=500, l=2, Bgbit=10, TRLWE 2^-24) is noisy by
+    design: its bootstrapping noise n (k+1) l N Var(digit) alpha^2 =
+    500 * 4 * 1024 * (2^18 / 3) * 2^-48 ~ 2^-10.6 (sigma ~ 0.025 turn) puts the
+    1/8-turn decision margin at ~4.3 sigma, i.e. about one failure per 10^5
+    gates in any exact implementation.  Both forms must show that noise and
+    no more: sigma of the output phase error in [0.02, 0.035] turn, the two
+    forms within 10 % of each other (the automatic split point s = 26 gives
+    about 4 %; s = 27 gave 15 %), at most 4 failures in 16384 gates."""
+    torch = torch_cuda
+    P = pkg.stress_params()
+    lwe, tlwe, ks, bk = pkg.gate_keyset(P, [0])
+    e = pkg.Engine(P)
+    try:
+        e.upload_bootstrapping_key(bk)
+        e.upload_keyswitch_key(ks)
+        total = 16384
+        rng = np.random.default_rng(96)
+        a = rng.integers(0, 2, total)
+        b = rng.integers(0, 2, total)
+        pkg.set_seed([96])
+        d_a = torch.from_numpy(pkg.encrypt_bits(P, a, lwe)).cuda()
+        d_b = torch.from_numpy(pkg.encrypt_bits(P, b, lwe)).cuda()
+        sig = {}
+        for form in ("split_fp32", "fp64"):
+            d_out = torch.empty_like(d_a)
+            e.bootsGate("NAND", d_out, d_a, d_b, total, form, stream=torch.cuda.current_stream().cuda_stream)
+            torch.cuda.synchronize()
+            e.synchronize()
+            out = d_out.cpu().numpy()
+            fails = int((pkg.decrypt_bits(P, out, lwe) != 1 - (a & b)).sum())
+            ph = pkg.phases(out, lwe).astype(np.int64)
+            want = np.where(1 - (a & b) == 1, 2 ** 29, -(2 ** 29))
+            err = ((ph - want + 2 ** 31) % 2 ** 32 - 2 ** 31) / 2.0 ** 32
+            sig[form] = float(err.std())
+            assert 0.02 <= sig[form] <= 0.035, (form, sig[form])
+            assert fails <= 4, (form, fails)
+        assert abs(sig["split_fp32"] / sig["fp64"] - 1) <= 0.10, sig
+        assert e.params.split_bits == 26
+    finally:
+        e.close()
