@@ -210,7 +210,7 @@ tfhe_gpu_status tfhe_gpu_tLweExtractLweSample(tfhe_gpu_ctx* ctx, int32_t* out,
                                               const int32_t* accum, int32_t count,
                                               void* stream);
 /* Key switch LWE(kN) -> LWE(n) with the context's key
- * (lwe-keyswitch-functions.cpp:228-241). */
+ * (lwe-keyswitch-functions.cpp:228-241).  out must not overlap in. */
 tfhe_gpu_status tfhe_gpu_lweKeySwitch(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* in,
                                       int32_t count, void* stream);
 /* Bootstrap without key switch: LWE(n) -> LWE(kN) with test vector mu
