@@ -179,7 +179,6 @@ class ClockSampler:
 def cpu_baseline(seconds, batch_hint):
     """The oracle (restated reference path) on all host cores, bounded."""
     from oracle import pyoracle
-    import __graft_entry__ as ge  # noqa: F401
     o = pyoracle.get()
     P = pyoracle.default_params()
     lwe, tlwe, ks, bk = o.gate_keyset(P, [0])
@@ -694,10 +693,8 @@ def main():
     e2e_value = job_throughput(batch * args.steps, world, e2e_total)
     lwe_bytes = batch * (P.n + 1) * 4
 
-    # dominant kernel alone: blind rotation + extraction on resident inputs
-    x = torch.empty_like(d_ca)
+    # dominant kernels alone: blind rotation + extraction on resident inputs
     u = torch.empty((batch, P.k * P.N + 1), dtype=torch.int32, device=dev)
-    lib.tfhe_gpu_bootsGate  # noqa: B018  (ensure symbol)
     kms = []
     for s in range(max(3, args.steps)):
         flush.fill_(s)
@@ -747,6 +744,19 @@ def main():
         extras["fp64_single_gate_ms"] = one
         extras["fp64_single_gate_bootstraps_per_s"] = 1000.0 / one
         extras["speedup_vs_fp64_single_gate"] = value / world / (1000.0 / one)
+        # key generation: host arithmetic vs the TGSW products on the GPU
+        # (same random values, same keys)
+        t0 = time.perf_counter()
+        host_keys = pkg.gate_keyset(P, [11])
+        t_host = time.perf_counter() - t0
+        kg = pkg.Engine(P, device=local)
+        t0 = time.perf_counter()
+        gpu_keys = kg.gate_keyset([11], forms=("split_fp32",))
+        torch.cuda.synchronize()
+        t_gpu = time.perf_counter() - t0
+        kg.close()
+        extras["keygen_s"] = {"host": t_host, "gpu_arithmetic_with_upload": t_gpu,
+                              "identical": all(bool((x == y).all()) for x, y in zip(host_keys, gpu_keys))}
         cpu = cpu_baseline(args.cpu_seconds, batch)
     else:
         cpu = None
