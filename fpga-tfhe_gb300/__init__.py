@@ -150,6 +150,7 @@ SIGNATURES = {
     "tfhe_client_encrypt_phases": (ctypes.c_int, [ctypes.c_void_p, I32P, ctypes.c_int32, I32P, I32P]),
     "tfhe_client_test_vector": (ctypes.c_int, [ctypes.c_int32, I32P, ctypes.c_int32, I32P]),
     "tfhe_gpu_gate_keyset": (ctypes.c_int, [VP, I32P, I32P, I32P, I32P, ctypes.c_uint32]),
+    "tfhe_gpu_selftest_timeout": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int32]),
     "tfhe_client_set_seed": (None, [U32P, ctypes.c_int32]),
     "tfhe_client_gate_keyset": (ctypes.c_int, [ctypes.c_void_p, I32P, I32P, I32P, I32P]),
     "tfhe_client_encrypt_bits": (ctypes.c_int, [ctypes.c_void_p, I32P, ctypes.c_int32, I32P, I32P]),
@@ -523,6 +524,12 @@ class Engine:
                                                   bk.ctypes.data_as(I32P) if want_bk else None, mask),
                     "gate_keyset")
         return lwe, tlwe, ks, bk
+
+    def selftest_timeout(self, form, count):
+        """Status of a blind rotation whose key stream never starts (the
+        bounded waits run out): 3 = TFHE_GPU_TIMEOUT, 0 for shapes without
+        waits."""
+        return self.lib.tfhe_gpu_selftest_timeout(self.ctx, self._form(form), int(count))
 
     def autotune(self, form, count):
         """Time the launch shapes on `count` ciphertexts; keeps and returns

@@ -729,7 +729,7 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
                                reinterpret_cast<const char*>(a.gsw), total_rows, 0};
     if (!INLINE && warp == 2 * GROUPS) {
         // producer warp: one lane streams all n * 2l key rows in order
-        if ((threadIdx.x & 31) == 0) {
+        if ((threadIdx.x & 31) == 0 && !a.stall_keys) {
             for (uint32_t r = 0; r < total_rows; ++r) {
                 keys.issue_upto(r);  // blocks on row r's slot, issues up to r + S - 1
                 if (keys.next_issue <= r) break;  // timed out
@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
     const int t = threadIdx.x & 63;
     const int c = blockIdx.x * GROUPS + g;
     if (g >= active) return;
-    keys.producer = INLINE && threadIdx.x == 0;
+    keys.producer = INLINE && threadIdx.x == 0 && !a.stall_keys;
 
     char* gbase = smem + Plan::group_off + (size_t)g * Plan::group;
     StepCtx<R, PARTS, 1> St;
@@ -949,7 +949,7 @@ __global__ void __launch_bounds__(128 * PAIRS, 1) k_blind_rotate_pair(KParams kp
     const int c = blockIdx.x * PAIRS + pr;
     if (pr >= active) return;
     const int n = kp.n;
-    RingKeys<R, PARTS, S> keys{ring, full, empty, 0, a.err, abort, threadIdx.x == 0,
+    RingKeys<R, PARTS, S> keys{ring, full, empty, 0, a.err, abort, threadIdx.x == 0 && !a.stall_keys,
                                reinterpret_cast<const char*>(a.gsw), (uint32_t)n * kpl, 0};
 
     char* pbase = smem + Plan::pair_off + (size_t)pr * Plan::pair;

@@ -837,6 +837,31 @@ tfhe_gpu_status tfhe_gpu_autotune(tfhe_gpu_ctx* ctx, tfhe_gpu_form form, int32_t
     return TFHE_GPU_OK;
 }
 
+tfhe_gpu_status tfhe_gpu_selftest_timeout(tfhe_gpu_ctx* ctx, tfhe_gpu_form form, int32_t count) {
+    CHECK_CTX(ctx);
+    if (count <= 0) return fail(ctx, TFHE_GPU_BAD_PARAM, "count");
+    RET(need_bk(ctx, form));
+    RET(check_device_status(ctx));  // start from a clean status word
+    const int n = ctx->P.n, nk = ctx->P.k * ctx->P.N;
+    void *x = nullptr, *u = nullptr;
+    RET(ensure_scratch(ctx, 0, (size_t)count * (n + 1) * sizeof(int32_t), &x));
+    RET(ensure_scratch(ctx, 1, (size_t)count * (nk + 1) * sizeof(int32_t), &u));
+    cudaStream_t st = ctx->stream;
+    CK(ctx, cudaMemsetAsync(x, 0, (size_t)count * (n + 1) * sizeof(int32_t), st));
+    EpArgs a{};
+    a.err = ctx->d_err;
+    a.x = (const int32_t*)x;
+    a.mu = tfhe_client_mod_switch_to_torus32(1, 8);
+    a.lwe_out = (int32_t*)u;
+    a.gsw = ctx->d_bk[form];
+    a.count = count;
+    a.stall_keys = 1;
+    CK(ctx, launch_external_product(ctx->dp, (Form)form, kEpBlindRotate, ctx->tables, a,
+                                    ctx->groups_per_cta[form], st));
+    CK(ctx, cudaStreamSynchronize(st));
+    return check_device_status(ctx);
+}
+
 tfhe_gpu_status tfhe_gpu_bootsMUX_host(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* a,
                                        const int32_t* b, const int32_t* c, int32_t count,
                                        tfhe_gpu_form form) {

@@ -80,6 +80,9 @@ struct EpArgs {
     // tv + c * tv_stride) instead of the constant mu; nullptr = constant mu
     const int32_t* tv;
     int32_t tv_stride;
+    // self-test of the bounded waits: the key-row ring's producer issues
+    // nothing, so every consumer wait runs out (tfhe_gpu_selftest_timeout)
+    int32_t stall_keys;
 };
 
 cudaError_t launch_external_product(const DevParams& P, Form f, EpMode mode,

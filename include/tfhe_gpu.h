@@ -278,6 +278,15 @@ tfhe_gpu_status tfhe_gpu_bootsGates_noalloc(tfhe_gpu_ctx* ctx, const int32_t* ga
                                             const int32_t* cb, int32_t count,
                                             tfhe_gpu_form form, void* stream);
 
+/* Self-test of the device-side failure path: runs one blind rotation of
+ * `count` samples with the current launch shape of `form` whose key-row
+ * stream is never started, so every bounded wait in the kernel runs out
+ * (after about 2 s; the first one to give up tells the rest of its CTA to
+ * stop waiting).  Returns what the host sees: TFHE_GPU_TIMEOUT for the
+ * shared-ring shapes; TFHE_GPU_OK for the L2-direct shapes, which have no
+ * waits.  The context stays usable.  No counterpart in the reference. */
+tfhe_gpu_status tfhe_gpu_selftest_timeout(tfhe_gpu_ctx* ctx, tfhe_gpu_form form, int32_t count);
+
 /* ---- CUDA graph of a gate batch; launch-shape autotuner ----------------- */
 /* Capture the whole gate pipeline of one batch (combination, blind rotation
  * and extraction, key switch) over fixed device buffers into a CUDA graph,

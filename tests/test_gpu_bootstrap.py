@@ -362,3 +362,68 @@ def test_stress_set_noise_band(pkg, torch_cuda):
         assert e.params.split_bits == 26
     finally:
         e.close()
+
+
+@pytest.mark.parametrize("groups,count", [(0, 8), (6, 6), (13, 5), (5, 5)])
+def test_bounded_waits_report_timeout(pkg, oracle, keys, torch_cuda, P, inputs, groups, count):
+    """The device-side failure path without a fault: a blind rotation whose
+    key-row stream never starts (a flag the producer honours) makes every
+    consumer's bounded wait run out; the kernel ends within a few seconds,
+    the host gets TFHE_GPU_TIMEOUT, and the same context then bootstraps
+    correctly.  Shapes: automatic (pair kernel), ring in line, pair, ring with
+    a producer warp."""
+    import time
+    torch = torch_cuda
+    e = pkg.Engine(pkg.default_params())
+    try:
+        e.upload_bootstrapping_key(keys["bk"], forms=("split_fp32",))
+        e.upload_keyswitch_key(keys["ks"])
+        e.set_groups_per_cta("split_fp32", groups)
+        t0 = time.perf_counter()
+        st = e.selftest_timeout("split_fp32", count)
+        took = time.perf_counter() - t0
+        assert st == 3, st
+        assert took < 30, took
+        e.synchronize()  # status word cleared: no stale timeout
+        a, b, ca, cb = inputs
+        d_out = torch.zeros((count, P.n + 1), dtype=torch.int32, device="cuda")
+        e.bootsGate("AND", d_out, dev(torch, ca[:count]), dev(torch, cb[:count]), count, "split_fp32",
+                    stream=cur(torch))
+        torch.cuda.synchronize()
+        e.synchronize()
+        assert (oracle.decrypt_bits(P, host(d_out), keys["lwe"]) == (a[:count] & b[:count])).all()
+    finally:
+        e.close()
+
+
+def test_l2_shape_has_no_waits(pkg, keys, torch_cuda):
+    e = pkg.Engine(pkg.default_params())
+    try:
+        e.upload_bootstrapping_key(keys["bk"], forms=("fp64",))
+        e.set_groups_per_cta("fp64", 3)
+        assert e.selftest_timeout("fp64", 3) == 0
+    finally:
+        e.close()
+
+
+@pytest.mark.parametrize("count", [456, 457, 912, 913, 1368, 1369])
+def test_auto_shape_boundaries(pkg, engine, oracle, keys, torch_cuda, P, count):
+    """Batch sizes on both sides of the automatic shape's boundaries (pair
+    only up to 3 per SM; ring waves of 6 per SM; ring + pair tail; ring +
+    a partial ring wave): every output decrypts to the truth."""
+    torch = torch_cuda
+    rng = np.random.default_rng(97 + count)
+    a = rng.integers(0, 2, count)
+    b = rng.integers(0, 2, count)
+    pkg.set_seed([97 + count])
+    ca = pkg.encrypt_bits(P, a, keys["lwe"])
+    cb = pkg.encrypt_bits(P, b, keys["lwe"])
+    gates = rng.integers(0, 10, count).astype(np.int32)
+    d_out = torch.zeros((count, P.n + 1), dtype=torch.int32, device="cuda")
+    engine.bootsGates(dev(torch, gates), d_out, dev(torch, ca), dev(torch, cb), count, "split_fp32",
+                      stream=cur(torch))
+    torch.cuda.synchronize()
+    engine.synchronize()
+    names = sorted(pyoracle.GATES, key=lambda g: pyoracle.GATES[g])
+    truth = np.array([pyoracle.GATE_FN[names[g]](x, y) for g, x, y in zip(gates, a, b)])
+    assert (pkg.decrypt_bits(P, host(d_out), keys["lwe"]) == truth).all()
