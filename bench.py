@@ -42,10 +42,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FLOP_PER_BOOTSTRAP = 162.6e6      # FFT-form algorithmic count, default set
-# DRAM bytes of the blind-rotation kernels, from the ncu capture in
-# profiles/blind_rotate_ring_pair_keyswitch_batch1000.md: every launch reads
-# the 61.9 MB key once (64.4 MB measured with the inputs of 912 gates), and
-# each ciphertext moves 2.5 KB in and 4.5 KB out.
+# DRAM bytes of the blind-rotation kernels, from a full ncu capture of the
+# ring and pair kernels on 1000 gates: every launch reads the 61.9 MB key
+# once (64.4 MB measured with the inputs of 912 gates), and each ciphertext
+# moves 2.5 KB in and 4.5 KB out.
 DRAM_KEY_BYTES_PER_LAUNCH = 61.9e6
 DRAM_IO_BYTES_PER_BOOTSTRAP = 2.52e3 + 4.5e3
 BATCH = 4096
@@ -787,7 +787,7 @@ def main():
                          "frac": achieved / peak,
                          "traffic": br_launches * DRAM_KEY_BYTES_PER_LAUNCH + batch * DRAM_IO_BYTES_PER_BOOTSTRAP,
                          "traffic_note": "DRAM bytes of the blind-rotation launches of one step, scaled from "
-                                         "the ncu capture of the same kernels (profiles/): key once per "
+                                         "an ncu capture of the same kernels on 1000 gates: key once per "
                                          "launch + per-ciphertext I/O",
                          "kernel": " + ".join(blind_rotate_kernels(args.form, eng.get_groups_per_cta(args.form),
                                                                    batch)) + " (blind rotation + extraction)",
