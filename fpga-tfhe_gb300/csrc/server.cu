@@ -1,4 +1,4 @@
-// server.cpp -- continuous-batching gate server over one engine context.
+// server.cu -- continuous-batching gate server over one engine context.
 //
 // The reference's test_bench server (test_bench/server/cloud.c:39-74) loads a
 // cloud key, reads ciphertexts, runs a circuit gate by gate (bootsOR,
@@ -76,6 +76,15 @@ __global__ void k_linear(int32_t* __restrict__ pool, const int32_t* __restrict__
         else if (c == (size_t)width - 1) v = mode == 2 ? (1 << 29) : -(1 << 29);
         pool[(size_t)dst * width + c] = v;
     }
+}
+
+// Latency records keep the most recent kLatencyKeep entries of each kind
+// (a long-running server would otherwise grow them without bound).
+constexpr size_t kLatencyKeep = size_t(1) << 22;
+
+void record(std::vector<double>& v, double x) {
+    if (v.size() >= 2 * kLatencyKeep) v.erase(v.begin(), v.end() - kLatencyKeep);
+    v.push_back(x);
 }
 
 int grid_for(size_t total) {
@@ -404,7 +413,7 @@ tfhe_gpu_status tfhe_gpu_server_step(tfhe_gpu_server* s, int32_t* ran) {
             p.c->done[p.g] = 1;
             p.c->ready[p.c->ninputs + p.g] = 1;
             p.c->remaining--;
-            if (boots) s->gate_latency.push_back(t1 - p.c->ready_at[p.g]);
+            if (boots) record(s->gate_latency, t1 - p.c->ready_at[p.g]);
         }
     };
     mark(lin, false);
@@ -428,7 +437,7 @@ tfhe_gpu_status tfhe_gpu_server_step(tfhe_gpu_server* s, int32_t* ran) {
         for (int32_t sl : c->slot) s->free_slots.push_back(sl);
         c->finished = now_s();
         c->is_done = true;
-        s->request_latency.push_back(c->finished - c->submitted);
+        record(s->request_latency, c->finished - c->submitted);
         s->finished[c->id] = std::move(it->second);
         it = s->active.erase(it);
     }

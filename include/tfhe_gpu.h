@@ -343,7 +343,8 @@ tfhe_gpu_status tfhe_gpu_server_poll(tfhe_gpu_server* srv, int64_t request_id, i
                                      int32_t* done, double* latency_s);
 /* stats[0..7]: queued, active, free slots, bootstraps run, busy seconds,
  * gate latencies recorded, request latencies recorded, pool slots; gate
- * (ready -> done) and request latencies copied up to cap[0], cap[1] entries. */
+ * (ready -> done) and request latencies copied up to cap[0], cap[1] entries
+ * (the server keeps the most recent 2^22 to 2^23 of each). */
 tfhe_gpu_status tfhe_gpu_server_stats(tfhe_gpu_server* srv, double* stats, double* gate_lat,
                                       double* req_lat, int64_t* cap);
 
