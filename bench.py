@@ -757,6 +757,7 @@ def main():
         kg.close()
         extras["keygen_s"] = {"host": t_host, "gpu_arithmetic_with_upload": t_gpu,
                               "identical": all(bool((x == y).all()) for x, y in zip(host_keys, gpu_keys))}
+        extras.update(side_paths(pkg, torch, eng, P, (lwe, tlwe, ks, bk), d_ca, d_cb, batch, stream, sp))
         cpu = cpu_baseline(args.cpu_seconds, batch)
     else:
         cpu = None
@@ -805,6 +806,55 @@ def main():
     eng.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def side_paths(pkg, torch, eng, P, keys, d_ca, d_cb, batch, stream, sp):
+    """Throughput of the paths either side of the gate bootstrap, on the same
+    batch: bootsMUX (two bootstraps and one key switch per output), the
+    programmable bootstrap with a lookup table, and the cloud-key file
+    (write, then read straight into a fresh context's device keys)."""
+    import tempfile
+    lwe, tlwe, ks, bk = keys
+    out = {}
+
+    def timed_ms(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1)
+            best = t if best is None or t < best else best
+        return best
+
+    d_out = torch.empty_like(d_ca)
+    # three independent inputs (a selector equal to an input would make one
+    # of the two bootstraps act on a noiseless trivial sample, which skips)
+    d_cc = d_cb.flip(0).contiguous()
+    ms = timed_ms(lambda: eng.bootsMUX(d_out, d_ca, d_cb, d_cc, batch, "split_fp32", stream=sp))
+    out["mux_outputs_per_s"] = batch / (ms / 1000.0)
+    out["mux_bootstraps_per_s"] = 2 * batch / (ms / 1000.0)
+    table = [pkg.mod_switch_to_torus32((3 * m + 1) % 8, 16) for m in range(8)]
+    d_tv = torch.from_numpy(pkg.test_vector(P.N, table)).cuda()
+    ms = timed_ms(lambda: eng.bootstrap_tv(d_out, d_ca, d_tv, batch, "split_fp32", stream=sp))
+    out["lookup_table_bootstraps_per_s"] = batch / (ms / 1000.0)
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "cloud.key")
+        t0 = time.perf_counter()
+        pkg.save_cloud_key(path, P, bk, ks)
+        t_save = time.perf_counter() - t0
+        size = os.path.getsize(path)
+        e2 = pkg.Engine(P, device=torch.cuda.current_device())
+        t0 = time.perf_counter()
+        e2.upload_cloud_key_file(path, forms=("split_fp32",))
+        t_load = time.perf_counter() - t0
+        e2.close()
+    out["cloud_key_file"] = {"bytes": size, "save_s": t_save, "load_to_device_s": t_load}
+    return out
 
 
 def blind_rotate_kernels(form, shape, batch, l=3):
