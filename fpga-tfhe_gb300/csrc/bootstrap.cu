@@ -84,30 +84,28 @@ __device__ __forceinline__ int32_t test_vector_coef(const EpArgs& a, int c, int 
 
 // Rounding the inverse transform's FP32 output to Torus32 without a float ->
 // int64 conversion (on this part that conversion issues to the narrow FP64
-// pipe): FP32 adds and FMAs plus integer adds.  M = 1.5 * 2^23: for |y| <
-// 2^22 the sum y + M rounds y to the nearest integer, whose two's complement
-// is then the low bits of the sum's encoding.
+// pipe).  M = 1.5 * 2^23: for |y| < 2^22 the sum y + M rounds y to the
+// nearest integer, whose two's complement is then the low bits of the sum's
+// encoding.
 constexpr float kRoundMagic = 12582912.0f;
 constexpr int32_t kRoundMagicBits = 0x4B400000;
 
 // round(v / 512) mod 2^32 for |v / 512| < 2^22 (the high key part's product:
-// about 2^18 typical, the exactness limit of FP32 is 2^24).
+// about 2^18 typical, the exactness limit of FP32 is 2^24): one FMA and one
+// integer add.
 __device__ __forceinline__ uint32_t round_small_u32(float v) {
     return (uint32_t)(__float_as_int(fmaf(v, 0x1p-9f, kRoundMagic)) - kRoundMagicBits);
 }
 
 // round(v / 512) mod 2^32 for any |v / 512| < 2^53 (the low key part's
-// product, up to about 2^36): remove the multiple of 2^32, then split the
-// remainder (|a| <= 2^31) into 2^16 a1 + a2 and round both pieces with the
-// magic constant.  Every step is exact in FP32.
+// product, up to about 2^36): the multiple of 2^32 is removed exactly in
+// FP32, and the remainder (|a / 512| <= 2^31) goes through a float -> int32
+// conversion, which does not use the FP64 pipe.  (A remainder of exactly
+// +2^31 saturates one unit short: an error of one unit in the low part.)
 __device__ __forceinline__ uint32_t round_wrap_u32(float v) {
     const float q = fmaf(v, 0x1p-41f, kRoundMagic) - kRoundMagic;  // rint(v / 2^41)
     const float a = fmaf(-q, 0x1p41f, v);                             // exact, |a| <= 2^40
-    const float u1 = fmaf(a, 0x1p-25f, kRoundMagic);                  // rint(a / 2^25) in the low bits
-    const float a2 = fmaf(-(u1 - kRoundMagic), 0x1p25f, a);           // exact, |a2| <= 2^24
-    const int32_t i1 = __float_as_int(u1) - kRoundMagicBits;
-    const int32_t i2 = __float_as_int(fmaf(a2, 0x1p-9f, kRoundMagic)) - kRoundMagicBits;
-    return ((uint32_t)i1 << 16) + (uint32_t)i2;
+    return (uint32_t)__float2int_rn(a * 0x1p-9f);
 }
 
 // Gadget digit of u at `decal` as a transform input: ((u >> decal) & mask) -
