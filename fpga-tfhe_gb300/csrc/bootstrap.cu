@@ -122,6 +122,33 @@ __device__ __forceinline__ R digit_value(uint32_t u, int decal, uint32_t mask, i
     }
 }
 
+// Both digits of a folded point (coefficients x and x + 512) as one
+// complex transform input; FP32: one packed subtraction.
+template <typename R>
+__device__ __forceinline__ cpx<R> digit_pair(uint32_t u0, uint32_t u1, int decal, uint32_t mask, int halfBg) {
+    if constexpr (sizeof(R) == 4) {
+        const float f0 = __int_as_float((int32_t)(((u0 >> decal) & mask) | (uint32_t)kRoundMagicBits));
+        const float f1 = __int_as_float((int32_t)(((u1 >> decal) & mask) | (uint32_t)kRoundMagicBits));
+        return unpk(__fadd2_rn(make_float2(f0, f1), bc(-(kRoundMagic + (float)halfBg))));
+    } else {
+        return {digit_value<R>(u0, decal, mask, halfBg), digit_value<R>(u1, decal, mask, halfBg)};
+    }
+}
+
+// round_small_u32 / round_wrap_u32 on both halves of a packed pair.
+__device__ __forceinline__ void round_small_pair(cpx<float> z, uint32_t& a0, uint32_t& a1) {
+    const float2 r = __ffma2_rn(pk(z), bc(0x1p-9f), bc(kRoundMagic));
+    a0 = (uint32_t)(__float_as_int(r.x) - kRoundMagicBits);
+    a1 = (uint32_t)(__float_as_int(r.y) - kRoundMagicBits);
+}
+__device__ __forceinline__ void round_wrap_pair(cpx<float> z, uint32_t& a0, uint32_t& a1) {
+    const float2 q = __fadd2_rn(__ffma2_rn(pk(z), bc(0x1p-41f), bc(kRoundMagic)), bc(-kRoundMagic));
+    const float2 a = __ffma2_rn(make_float2(-q.x, -q.y), bc(0x1p41f), pk(z));
+    const float2 sc = __fmul2_rn(a, bc(0x1p-9f));
+    a0 = (uint32_t)__float2int_rn(sc.x);
+    a1 = (uint32_t)__float2int_rn(sc.y);
+}
+
 template <typename R>
 __device__ __forceinline__ int64_t to_int(R v);
 template <>
@@ -236,14 +263,14 @@ __device__ __forceinline__ void mac_row(cpx<R> (&out)[2][PARTS][8], const cpx<R>
                 for (int qq = 0; qq < 4; ++qq) {
                     const float4 w = key_load4<SHARED>(g4 + qq * 64 + t);
                     const cpx<R> k0 = {(R)w.x, (R)w.y}, k1 = {(R)w.z, (R)w.w};
-                    out[j][pt][2 * qq] = cadd(out[j][pt][2 * qq], cmul(v[2 * qq], k0));
-                    out[j][pt][2 * qq + 1] = cadd(out[j][pt][2 * qq + 1], cmul(v[2 * qq + 1], k1));
+                    out[j][pt][2 * qq] = cmac(out[j][pt][2 * qq], v[2 * qq], k0);
+                    out[j][pt][2 * qq + 1] = cmac(out[j][pt][2 * qq + 1], v[2 * qq + 1], k1);
                 }
             } else {
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
                     const cpx<R> k0 = gk[key_index<R>(t, q)];
-                    out[j][pt][q] = cadd(out[j][pt][q], cmul(v[q], k0));
+                    out[j][pt][q] = cmac(out[j][pt][q], v[q], k0);
                 }
             }
         }
@@ -290,9 +317,7 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
 #pragma unroll
                 for (int b = 0; b < FB; ++b) {
                     const int decal = 32 - (lev0 + b + 1) * S.Bgbit;
-                    const int d0 = (int)((r0[r] >> decal) & mask) - halfBg;
-                    const int d1 = (int)((r1[r] >> decal) & mask) - halfBg;
-                    v[b][r] = cpx<R>{(R)d0, (R)d1};
+                    v[b][r] = digit_pair<R>(r0[r], r1[r], decal, mask, halfBg);
                 }
             }
             fft512_forward_tw_multi<FB>(v, *reinterpret_cast<const FftScratch<R>(*)[FB]>(S.s), S.tw, S.ix, t,
@@ -328,13 +353,8 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
                     const cpx<R> z = v[b][q];
                     uint32_t a0, a1;
                     if constexpr (sizeof(R) == 4) {
-                        if (PARTS == 2 && pt == 0) {
-                            a0 = round_small_u32(z.x);
-                            a1 = round_small_u32(z.y);
-                        } else {
-                            a0 = round_wrap_u32(z.x);
-                            a1 = round_wrap_u32(z.y);
-                        }
+                        if (PARTS == 2 && pt == 0) round_small_pair(z, a0, a1);
+                        else round_wrap_pair(z, a0, a1);
                     } else {
                         a0 = (uint32_t)(uint64_t)to_int<R>(z.x * inv);
                         a1 = (uint32_t)(uint64_t)to_int<R>(z.y * inv);
@@ -379,21 +399,22 @@ __device__ __forceinline__ void round_part(const cpx<R> (&v)[8], int pt, int spl
         if (PARTS == 2 && pt == 0) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                c0[q] = round_small_u32(v[q].x) << split;
-                c1[q] = round_small_u32(v[q].y) << split;
+                uint32_t a0, a1;
+                round_small_pair(v[q], a0, a1);
+                c0[q] = a0 << split;
+                c1[q] = a1 << split;
             }
         } else if (PARTS == 2) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                c0[q] += round_wrap_u32(v[q].x);
-                c1[q] += round_wrap_u32(v[q].y);
+                uint32_t a0, a1;
+                round_wrap_pair(v[q], a0, a1);
+                c0[q] += a0;
+                c1[q] += a1;
             }
         } else {
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                c0[q] = round_wrap_u32(v[q].x);
-                c1[q] = round_wrap_u32(v[q].y);
-            }
+            for (int q = 0; q < 8; ++q) round_wrap_pair(v[q], c0[q], c1[q]);
         }
     } else {
         const R inv = (R)(1.0 / 512.0);
@@ -465,8 +486,7 @@ __device__ __forceinline__ void ep_step_lean(const StepCtx<R, PARTS, 1>& S, Keys
             cpx<R> v[8];
 #pragma unroll
             for (int r = 0; r < 8; ++r)
-                v[r] = cpx<R>{digit_value<R>(r0[r], decal, mask, halfBg),
-                              digit_value<R>(r1[r], decal, mask, halfBg)};
+                v[r] = digit_pair<R>(r0[r], r1[r], decal, mask, halfBg);
             fft512_forward_tw(v, S.s[0], S.tw, S.ix, t, S.bar_id);
             const int p = jp * L + lev;
             mac_row<R, PARTS, Keys::kShared>(out, v, keys.acquire(p), t);
@@ -848,8 +868,7 @@ __device__ __forceinline__ void ep_step_half(const StepCtx<R, PARTS, 1>& S, Keys
             const int decal = 32 - (lev + 1) * S.Bgbit;
 #pragma unroll
             for (int r = 0; r < 8; ++r)
-                v[r] = cpx<R>{digit_value<R>(r0[r], decal, mask, halfBg),
-                              digit_value<R>(r1[r], decal, mask, halfBg)};
+                v[r] = digit_pair<R>(r0[r], r1[r], decal, mask, halfBg);
             fft512_forward_tw(v, S.s[0], S.tw, S.ix, t, S.bar_id);
             const int p = h * L + lev;
             mac_row<R, PARTS, Keys::kShared>(out, v, keys.acquire(p), t);

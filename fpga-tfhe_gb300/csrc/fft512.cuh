@@ -51,6 +51,44 @@ template <typename R>
 __device__ __forceinline__ cpx<R> cmulc(cpx<R> a, cpx<R> b) {
     return {a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
 }
+// acc + a * w
+template <typename R>
+__device__ __forceinline__ cpx<R> cmac(cpx<R> acc, cpx<R> a, cpx<R> w) {
+    return cadd(acc, cmul(a, w));
+}
+
+// ---- FP32: packed pair arithmetic ---------------------------------------
+// A complex float is one 64-bit register pair and add/mul/fma.f32x2 (sm_100
+// and later) work on both halves in one instruction, so complex adds take
+// one instruction and complex products two.  Measured on GB300 (instruction
+// counts of isolated loops): a whole-pair negation, a broadcast {x, x} of
+// one half and the swap-and-negate {-y, x} of i * a cost nothing extra as
+// multiplicands; an FMA by a literal +-1 becomes an add, and an add whose
+// addend is swapped costs about one more instruction, so i-multiplied
+// addends inside the radix-8 butterfly stay scalar.
+__device__ __forceinline__ float2 pk(cpx<float> a) { return make_float2(a.x, a.y); }
+__device__ __forceinline__ cpx<float> unpk(float2 a) { return {a.x, a.y}; }
+__device__ __forceinline__ float2 bc(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 times_i(cpx<float> a) { return make_float2(-a.y, a.x); }
+__device__ __forceinline__ float2 times_minus_i(cpx<float> a) { return make_float2(a.y, -a.x); }
+
+__device__ __forceinline__ cpx<float> cadd(cpx<float> a, cpx<float> b) {
+    return unpk(__fadd2_rn(pk(a), pk(b)));
+}
+__device__ __forceinline__ cpx<float> csub(cpx<float> a, cpx<float> b) {
+    return unpk(__fadd2_rn(pk(a), make_float2(-b.x, -b.y)));
+}
+// a w = w.x a + w.y (i a)
+__device__ __forceinline__ cpx<float> cmul(cpx<float> a, cpx<float> w) {
+    return unpk(__ffma2_rn(times_i(a), bc(w.y), __fmul2_rn(pk(a), bc(w.x))));
+}
+// a conj(w) = w.x a + w.y (-i a)
+__device__ __forceinline__ cpx<float> cmulc(cpx<float> a, cpx<float> w) {
+    return unpk(__ffma2_rn(times_minus_i(a), bc(w.y), __fmul2_rn(pk(a), bc(w.x))));
+}
+__device__ __forceinline__ cpx<float> cmac(cpx<float> acc, cpx<float> a, cpx<float> w) {
+    return unpk(__ffma2_rn(times_i(a), bc(w.y), __ffma2_rn(pk(a), bc(w.x), pk(acc))));
+}
 
 constexpr int kFftPoints = 512;
 constexpr int kFftThreads = 64;
@@ -75,39 +113,77 @@ __device__ __forceinline__ int slot<float>(int p) {
 template <>
 __device__ __forceinline__ int slot<double>(int p) { return spad(p); }
 
-// 8-point DFT, y_q = sum_r v_r w^{rq}, w = e^{S 2 pi i / 8}.
-template <int S, typename R>
-__device__ __forceinline__ void dft8(cpx<R> (&v)[8]) {
-    const R h = (R)0.70710678118654752440084436210485;
-    cpx<R> b[8];
+// FP32 8-point DFT on packed pairs: the same butterflies as dft8 below, the
+// multiplications by w and w^3 as two packed instructions each, the
+// i-multiplied terms (w^2 and the last stage's e3) as scalar adds.
+template <int S>
+__device__ __forceinline__ void dft8_f32(cpx<float> (&v)[8]) {
+    constexpr float h = 0.70710678118654752440f;
+    cpx<float> b[8];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         b[r] = cadd(v[r], v[r + 4]);
         b[r + 4] = csub(v[r], v[r + 4]);
     }
-    {  // b5 *= w = (1 + S i) h
-        const R x = b[5].x, y = b[5].y;
-        b[5] = {(x - S * y) * h, (y + S * x) * h};
+    // b5 *= (1 + S i) h = h b5 + S h (i b5);  b7 *= (-1 + S i) h
+    b[5] = unpk(__ffma2_rn(times_i(b[5]), bc(S * h), __fmul2_rn(pk(b[5]), bc(h))));
+    b[7] = unpk(__ffma2_rn(times_i(b[7]), bc(S * h), __fmul2_rn(make_float2(-b[7].x, -b[7].y), bc(h))));
+    {  // c = b0, b1, b2, b3
+        const cpx<float> e0 = cadd(b[0], b[2]), e1 = csub(b[0], b[2]);
+        const cpx<float> e2 = cadd(b[1], b[3]), d = csub(b[1], b[3]);
+        v[0] = cadd(e0, e2);
+        v[4] = csub(e0, e2);
+        v[2] = {e1.x - S * d.y, e1.y + S * d.x};  // e1 + S i d
+        v[6] = {e1.x + S * d.y, e1.y - S * d.x};
     }
-    {  // b6 *= w^2 = S i
-        const R x = b[6].x, y = b[6].y;
-        b[6] = {-S * y, S * x};
+    {  // c = b4, b5, S i b6, b7
+        const cpx<float> e0 = {b[4].x - S * b[6].y, b[4].y + S * b[6].x};
+        const cpx<float> e1 = {b[4].x + S * b[6].y, b[4].y - S * b[6].x};
+        const cpx<float> e2 = cadd(b[5], b[7]), d = csub(b[5], b[7]);
+        v[1] = cadd(e0, e2);
+        v[5] = csub(e0, e2);
+        v[3] = {e1.x - S * d.y, e1.y + S * d.x};
+        v[7] = {e1.x + S * d.y, e1.y - S * d.x};
     }
-    {  // b7 *= w^3 = (-1 + S i) h
-        const R x = b[7].x, y = b[7].y;
-        b[7] = {(-x - S * y) * h, (S * x - y) * h};
-    }
+}
+
+// 8-point DFT, y_q = sum_r v_r w^{rq}, w = e^{S 2 pi i / 8}.
+template <int S, typename R>
+__device__ __forceinline__ void dft8(cpx<R> (&v)[8]) {
+    if constexpr (sizeof(R) == 4) {
+        dft8_f32<S>(v);
+    } else {
+        const R h = (R)0.70710678118654752440084436210485;
+        cpx<R> b[8];
 #pragma unroll
-    for (int half = 0; half < 2; ++half) {
-        const cpx<R> c0 = b[4 * half + 0], c1 = b[4 * half + 1];
-        const cpx<R> c2 = b[4 * half + 2], c3 = b[4 * half + 3];
-        const cpx<R> e0 = cadd(c0, c2), e1 = csub(c0, c2), e2 = cadd(c1, c3);
-        const cpx<R> d = csub(c1, c3);
-        const cpx<R> e3 = {-S * d.y, S * d.x};
-        v[half + 0] = cadd(e0, e2);
-        v[half + 2] = cadd(e1, e3);
-        v[half + 4] = csub(e0, e2);
-        v[half + 6] = csub(e1, e3);
+        for (int r = 0; r < 4; ++r) {
+            b[r] = cadd(v[r], v[r + 4]);
+            b[r + 4] = csub(v[r], v[r + 4]);
+        }
+        {  // b5 *= w = (1 + S i) h
+            const R x = b[5].x, y = b[5].y;
+            b[5] = {(x - S * y) * h, (y + S * x) * h};
+        }
+        {  // b6 *= w^2 = S i
+            const R x = b[6].x, y = b[6].y;
+            b[6] = {-S * y, S * x};
+        }
+        {  // b7 *= w^3 = (-1 + S i) h
+            const R x = b[7].x, y = b[7].y;
+            b[7] = {(-x - S * y) * h, (S * x - y) * h};
+        }
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const cpx<R> c0 = b[4 * half + 0], c1 = b[4 * half + 1];
+            const cpx<R> c2 = b[4 * half + 2], c3 = b[4 * half + 3];
+            const cpx<R> e0 = cadd(c0, c2), e1 = csub(c0, c2), e2 = cadd(c1, c3);
+            const cpx<R> d = csub(c1, c3);
+            const cpx<R> e3 = {-S * d.y, S * d.x};
+            v[half + 0] = cadd(e0, e2);
+            v[half + 2] = cadd(e1, e3);
+            v[half + 4] = csub(e0, e2);
+            v[half + 6] = csub(e1, e3);
+        }
     }
 }
 
