@@ -864,14 +864,18 @@ def blind_rotate_kernels(form, shape, batch, l=3):
         return (["k_external_product<double,1,BlindRotate,3,%d>" % l] if shape == 3
                 else ["k_blind_rotate_ring<double,1,4,%d,4,inline>" % l])
     ring = "k_blind_rotate_ring<float,2,%d,%d,4,%s>"
+    batched = "k_blind_rotate_ring<float,2,%d,%d,4,inline,nb%d>"
     pair = "k_blind_rotate_pair<float,2,%d,%d,4>"
+    nb = max(l, 2)
     if shape == 0:
-        wave = 6 * SMS
+        wave = 4 * SMS
         full, rest = (batch // wave) * wave, batch - (batch // wave) * wave
-        if rest == 0 or rest > 3 * SMS:
-            return [ring % (6, l, "inline")]
-        names = [ring % (6, l, "inline") + " x %d" % full] if full else []
+        if rest == 0 or rest > 2 * SMS:
+            return [batched % (4, l, nb)]
+        names = [batched % (4, l, nb) + " x %d" % full] if full else []
         return names + [pair % ((rest + SMS - 1) // SMS, l) + " x %d" % rest]
+    if shape in (9, 10):
+        return [batched % (13 - shape, l, nb)]
     if shape in (11, 12, 13):
         return [pair % (shape - 10, l)]
     if shape in (1, 2, 4):

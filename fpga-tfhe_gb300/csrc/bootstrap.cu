@@ -704,7 +704,7 @@ struct RingKeys {
     __device__ __forceinline__ void release(int p) const { mbar_arrive(&empty[(row0 + (uint32_t)p) % S]); }
 };
 
-template <typename R, int PARTS, int GROUPS, int L, int S>
+template <typename R, int PARTS, int GROUPS, int L, int S, int NB = 1>
 struct RingPlan {
     static constexpr size_t kRowBytes = (size_t)2 * PARTS * kHalf * sizeof(cpx<R>);
     static constexpr size_t tables = kHotSize * sizeof(cpx<R>);
@@ -713,14 +713,18 @@ struct RingPlan {
     static constexpr size_t flag_off = bar_off + 2 * S * sizeof(uint64_t);
     static constexpr size_t group_off = (flag_off + sizeof(int) + 127) & ~(size_t)127;
     static constexpr size_t acc = 2 * kN * sizeof(int32_t);
-    static constexpr size_t group = acc + 2 * kScratchStride * sizeof(cpx<R>);
+    static constexpr size_t group = acc + NB * 2 * kScratchStride * sizeof(cpx<R>);
     static constexpr size_t total = group_off + GROUPS * group;
 };
 
-template <typename R, int PARTS, int GROUPS, int L, int S, bool INLINE>
+// NB = 1: one transform at a time (ep_step_lean).  NB > 1: the l forward
+// and the PARTS inverse transforms of a step run together (ep_step), which
+// needs NB exchange buffer pairs per group and about 250 registers, so at
+// most four groups per CTA.
+template <typename R, int PARTS, int GROUPS, int L, int S, bool INLINE, int NB = 1>
 __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
     k_blind_rotate_ring(KParams kp, Tables T, EpArgs a) {
-    using Plan = RingPlan<R, PARTS, GROUPS, L, S>;
+    using Plan = RingPlan<R, PARTS, GROUPS, L, S, NB>;
     constexpr int kpl = 2 * L;
     extern __shared__ __align__(128) char smem[];
     cpx<R>* tables = reinterpret_cast<cpx<R>*>(smem);
@@ -764,11 +768,13 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
     keys.producer = INLINE && threadIdx.x == 0 && !a.stall_keys;
 
     char* gbase = smem + Plan::group_off + (size_t)g * Plan::group;
-    StepCtx<R, PARTS, 1> St;
+    StepCtx<R, PARTS, NB> St;
     St.tw = hot_twiddles<R>(tables);
     St.ix = make_fft_idx(t);
     St.acc = reinterpret_cast<int32_t*>(gbase);
-    St.s[0] = scratch_at<R>(gbase + Plan::acc);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+        St.s[b] = scratch_at<R>(gbase + Plan::acc + (size_t)b * 2 * kScratchStride * sizeof(cpx<R>));
     St.t = t;
     St.bar_id = 1 + g;
     St.Bgbit = kp.Bgbit;
@@ -802,7 +808,8 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
             }
             continue;
         }
-        ep_step_lean<R, PARTS, L>(St, keys, ai);
+        if constexpr (NB == 1) ep_step_lean<R, PARTS, L>(St, keys, ai);
+        else ep_step<R, PARTS, true, L, L, PARTS, NB>(St, keys, ai);
     }
     if (keys.producer) keys.drain();
     if (a.acc_out) {
@@ -1362,12 +1369,12 @@ cudaError_t launch_ep_t(const DevParams& P, const Tables& T, const EpArgs& a, cu
     return cudaGetLastError();
 }
 
-template <typename R, int PARTS, int GROUPS, int L, bool INLINE, int S = 4>
+template <typename R, int PARTS, int GROUPS, int L, bool INLINE, int S = 4, int NB = 1>
 cudaError_t launch_ring_t(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
     if (a.count <= 0) return cudaSuccess;
     const KParams kp = make_kparams(P);
-    using Plan = RingPlan<R, PARTS, GROUPS, L, S>;
-    auto kern = k_blind_rotate_ring<R, PARTS, GROUPS, L, S, INLINE>;
+    using Plan = RingPlan<R, PARTS, GROUPS, L, S, NB>;
+    auto kern = k_blind_rotate_ring<R, PARTS, GROUPS, L, S, INLINE, NB>;
     cudaError_t e = set_smem(kern, Plan::total);
     if (e != cudaSuccess) return e;
     const int grid = (a.count + GROUPS - 1) / GROUPS;
@@ -1400,18 +1407,25 @@ cudaError_t launch_pair_fp32(const DevParams& P, const Tables& T, const EpArgs& 
 }
 
 // Automatic shape of a split-FP32 blind rotation over `count` ciphertexts:
-// whole waves of six ciphertexts per SM on the shared-ring kernel; a
-// remainder of at most three per SM on the pair kernel (two halves per
-// ciphertext, about half the time per ciphertext), so the last partial wave
-// takes half a wave; a larger remainder as one more ring wave.
+// whole waves of four ciphertexts per SM on the shared-ring kernel with a
+// step's transforms run together; a remainder of at most two per SM on the
+// pair kernel (two halves per ciphertext: measured 2.6 ms for one and 3.3 ms
+// for two per SM against 4.5 ms for a ring wave of any fill); a larger
+// remainder as one more ring wave (4.5 ms for three per SM, the pair kernel
+// 5.1 ms).
+template <int L>
+cudaError_t launch_ring_batched(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
+    return launch_ring_t<float, 2, 4, L, true, 4, (L > 2 ? L : 2)>(P, T, a, st);
+}
+
 template <int L>
 cudaError_t launch_auto_fp32(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
-    const int wave = 6 * kSmCount;
+    const int wave = 4 * kSmCount;
     const int full = (a.count / wave) * wave;
     const int rest = a.count - full;
-    if (rest == 0 || rest > 3 * kSmCount) return launch_ring_t<float, 2, 6, L, true>(P, T, a, st);
+    if (rest == 0 || rest > 2 * kSmCount) return launch_ring_batched<L>(P, T, a, st);
     if (full) {
-        cudaError_t e = launch_ring_t<float, 2, 6, L, true>(P, T, slice_blind_rotate(P, a, 0, full), st);
+        cudaError_t e = launch_ring_batched<L>(P, T, slice_blind_rotate(P, a, 0, full), st);
         if (e != cudaSuccess) return e;
     }
     const int per_cta = (rest + kSmCount - 1) / kSmCount;
@@ -1439,8 +1453,11 @@ cudaError_t launch_ep_l(const DevParams& P, Form f, EpMode mode, const Tables& T
         if (groups == 0) return launch_auto_fp32<L>(P, T, a, st);
         // 1, 2, 4: L2-direct key reads; 5: shared ring fed by a producer
         // warp; 6, 7, 8: shared ring fed in line by one consumer thread;
-        // 11, 12, 13: pair kernel with 1, 2, 3 ciphertexts per CTA
+        // 9, 10: shared ring with a step's transforms run together, 4 or 3
+        // groups; 11, 12, 13: pair kernel with 1, 2, 3 ciphertexts per CTA
         if (groups >= 11 && groups <= 13) return launch_pair_fp32<L>(P, T, a, groups - 10, st);
+        if (groups == 9) return launch_ring_batched<L>(P, T, a, st);
+        if (groups == 10) return launch_ring_t<float, 2, 3, L, true, 4, (L > 2 ? L : 2)>(P, T, a, st);
         if (groups == 1) return launch_ep_t<float, 2, kEpBlindRotate, 1, L>(P, T, a, st);
         if (groups == 2) return launch_ep_t<float, 2, kEpBlindRotate, 2, L>(P, T, a, st);
         if (groups == 4) return launch_ep_t<float, 2, kEpBlindRotate, 4, L>(P, T, a, st);

@@ -399,32 +399,46 @@ __device__ __forceinline__ cpx<R> twist_c(int r) {
 
 // In: v[r] = untwisted folded point t + 64r.  Out: v[q] = position 8t + q
 // of the transform of the twisted sequence.  tw.a = psi^t W^(tq) table.
+// With NB > 1 every twiddle is loaded once and applied to all NB point sets
+// (the compiler cannot merge the loads across the exchange stores).
 template <int NB, typename R>
 __device__ __forceinline__ void fft512_forward_tw_multi(cpx<R> (&v)[NB][8], const FftScratch<R> (&s)[NB],
                                                         const FftTwiddles<R>& tw, const FftIdx& ix, int t,
-                                                  int bar_id) {
+                                                        int bar_id) {
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
         for (int r = 1; r < 8; ++r) v[b][r] = cmul(v[b][r], twist_c<R>(r));
         dft8<1>(v[b]);
+    }
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.a[q * 64 + t]);
+    for (int q = 0; q < 8; ++q) {
+        const cpx<R> w = tw.a[q * 64 + t];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) v[b][q] = cmul(v[b][q], w);
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
 #pragma unroll
         for (int q = 0; q < 8; ++q) s[b].b0[slot_a<R>(ix, t, q)] = v[b][q];
-    }
     group_sync(bar_id);
-    const int hb = t >> 3, j = t & 7;
+    const int j = t & 7;
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
         for (int r = 0; r < 8; ++r) v[b][r] = s[b].b0[slot_b<R>(ix, t, r)];
         dft8<1>(v[b]);
+    }
 #pragma unroll
-        for (int q = 1; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.b[q * 8 + j]);
+    for (int q = 1; q < 8; ++q) {
+        const cpx<R> w = tw.b[q * 8 + j];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) v[b][q] = cmul(v[b][q], w);
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
 #pragma unroll
         for (int q = 0; q < 8; ++q) s[b].b1[slot_b<R>(ix, t, q)] = v[b][q];
-    }
     group_sync(bar_id);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
@@ -439,7 +453,7 @@ __device__ __forceinline__ void fft512_forward_tw_multi(cpx<R> (&v)[NB][8], cons
 template <int NB, typename R>
 __device__ __forceinline__ void fft512_inverse_tw_multi(cpx<R> (&v)[NB][8], const FftScratch<R> (&s)[NB],
                                                         const FftTwiddles<R>& tw, const FftIdx& ix, int t,
-                                                  int bar_id) {
+                                                        int bar_id) {
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
         dft8<-1>(v[b]);
@@ -447,23 +461,33 @@ __device__ __forceinline__ void fft512_inverse_tw_multi(cpx<R> (&v)[NB][8], cons
         for (int q = 0; q < 8; ++q) s[b].b0[slot_c<R>(ix, t, q)] = v[b][q];
     }
     group_sync(bar_id);
-    const int hb = t >> 3, j = t & 7;
+    const int j = t & 7;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        if (r == 0) {
+#pragma unroll
+            for (int b = 0; b < NB; ++b) v[b][0] = s[b].b0[slot_b<R>(ix, t, 0)];
+        } else {
+            const cpx<R> w = tw.b[r * 8 + j];
+#pragma unroll
+            for (int b = 0; b < NB; ++b) v[b][r] = cmulc(s[b].b0[slot_b<R>(ix, t, r)], w);
+        }
+    }
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            v[b][r] = s[b].b0[slot_b<R>(ix, t, r)];
-            if (r) v[b][r] = cmulc(v[b][r], tw.b[r * 8 + j]);
-        }
         dft8<-1>(v[b]);
 #pragma unroll
         for (int q = 0; q < 8; ++q) s[b].b1[slot_b<R>(ix, t, q)] = v[b][q];
     }
     group_sync(bar_id);
 #pragma unroll
-    for (int b = 0; b < NB; ++b) {
+    for (int r = 0; r < 8; ++r) {
+        const cpx<R> w = tw.a[r * 64 + t];
 #pragma unroll
-        for (int r = 0; r < 8; ++r) v[b][r] = cmulc(s[b].b1[slot_a<R>(ix, t, r)], tw.a[r * 64 + t]);
+        for (int b = 0; b < NB; ++b) v[b][r] = cmulc(s[b].b1[slot_a<R>(ix, t, r)], w);
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
         dft8<-1>(v[b]);
 #pragma unroll
         for (int q = 1; q < 8; ++q) v[b][q] = cmulc(v[b][q], twist_c<R>(q));

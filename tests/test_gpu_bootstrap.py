@@ -227,8 +227,9 @@ def test_errors_are_status_codes(pkg, keys, torch_cuda, P):
 
 @pytest.mark.parametrize("form,groups", [("split_fp32", 0), ("split_fp32", 1), ("split_fp32", 2),
                                          ("split_fp32", 4), ("split_fp32", 5), ("split_fp32", 6),
-                                         ("split_fp32", 7), ("split_fp32", 8),
-                                         ("split_fp32", 11), ("split_fp32", 12), ("split_fp32", 13),
+                                         ("split_fp32", 7), ("split_fp32", 8), ("split_fp32", 9),
+                                         ("split_fp32", 10), ("split_fp32", 11), ("split_fp32", 12),
+                                         ("split_fp32", 13),
                                          ("fp64", 3), ("fp64", 4)])
 def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, groups):
     """Each blind-rotation launch shape (L2-direct and shared-ring kernels) on
@@ -260,12 +261,13 @@ def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, grou
 
 
 def test_auto_shape_full_wave_and_tail(pkg, oracle, keys, torch_cuda, P, inputs):
-    """The automatic split-FP32 shape on one full wave (6 per SM on the ring
-    kernel) plus a tail of 40 on the pair kernel: every output decrypts to the
-    truth and ciphertexts from both launches match the oracle's phases."""
+    """The automatic split-FP32 shape on one full wave (4 per SM on the
+    batched ring kernel) plus a tail of 40 on the pair kernel: every output
+    decrypts to the truth and ciphertexts from both launches match the
+    oracle's phases."""
     torch = torch_cuda
     a, b, ca, cb = inputs
-    count = 6 * 152 + 40
+    count = 4 * 152 + 40
     reps = (count + len(a) - 1) // len(a)
     a, b = np.tile(a, reps)[:count], np.tile(b, reps)[:count]
     ca, cb = np.tile(ca, (reps, 1))[:count], np.tile(cb, (reps, 1))[:count]
@@ -286,7 +288,7 @@ def test_auto_shape_full_wave_and_tail(pkg, oracle, keys, torch_cuda, P, inputs)
     names = sorted(pyoracle.GATES, key=lambda g: pyoracle.GATES[g])
     truth = np.array([pyoracle.GATE_FN[names[g]](x, y) for g, x, y in zip(gates, a, b)])
     assert (oracle.decrypt_bits(P, got, keys["lwe"]) == truth).all()
-    idx = np.array([0, 1, 911, 912, 913, count - 1])
+    idx = np.array([0, 1, 607, 608, 609, count - 1])
     ref = oracle.boots_gate_batch(P, keys["bk_fft"], keys["ks"], gates[idx], ca[idx], cb[idx])
     d = wrap_diff(oracle.phases(got[idx], keys["lwe"], P.n), oracle.phases(ref, keys["lwe"], P.n))
     assert np.abs(d).max() <= PHASE_TOL
@@ -364,14 +366,14 @@ def test_stress_set_noise_band(pkg, torch_cuda):
         e.close()
 
 
-@pytest.mark.parametrize("groups,count", [(0, 8), (6, 6), (13, 5), (5, 5)])
+@pytest.mark.parametrize("groups,count", [(0, 8), (6, 6), (9, 9), (13, 5), (5, 5)])
 def test_bounded_waits_report_timeout(pkg, oracle, keys, torch_cuda, P, inputs, groups, count):
     """The device-side failure path without a fault: a blind rotation whose
     key-row stream never starts (a flag the producer honours) makes every
     consumer's bounded wait run out; the kernel ends within a few seconds,
     the host gets TFHE_GPU_TIMEOUT, and the same context then bootstraps
-    correctly.  Shapes: automatic (pair kernel), ring in line, pair, ring with
-    a producer warp."""
+    correctly.  Shapes: automatic (pair kernel), ring in line, batched ring,
+    pair, ring with a producer warp."""
     import time
     torch = torch_cuda
     e = pkg.Engine(pkg.default_params())
@@ -406,11 +408,12 @@ def test_l2_shape_has_no_waits(pkg, keys, torch_cuda):
         e.close()
 
 
-@pytest.mark.parametrize("count", [456, 457, 912, 913, 1368, 1369])
+@pytest.mark.parametrize("count", [304, 305, 608, 609, 912, 913])
 def test_auto_shape_boundaries(pkg, engine, oracle, keys, torch_cuda, P, count):
     """Batch sizes on both sides of the automatic shape's boundaries (pair
-    only up to 3 per SM; ring waves of 6 per SM; ring + pair tail; ring +
-    a partial ring wave): every output decrypts to the truth."""
+    only up to 2 per SM; a partial ring wave above that; ring waves of 4 per
+    SM; ring + pair tail; ring + a partial ring wave): every output decrypts
+    to the truth."""
     torch = torch_cuda
     rng = np.random.default_rng(97 + count)
     a = rng.integers(0, 2, count)
