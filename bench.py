@@ -731,6 +731,10 @@ def main():
             torch.cuda.synchronize()
             one_ms.append(e0.elapsed_time(e1))
         one = statistics.median(one_ms[1:])
+        # a single gate on the automatic shape (pair kernel), whatever shape
+        # the autotuner kept for the full batch
+        tuned = eng.get_groups_per_cta("split_fp32")
+        eng.set_groups_per_cta("split_fp32", 0)
         one32 = []
         for s in range(4):
             e0 = torch.cuda.Event(enable_timing=True)
@@ -740,6 +744,7 @@ def main():
             e1.record(stream)
             torch.cuda.synchronize()
             one32.append(e0.elapsed_time(e1))
+        eng.set_groups_per_cta("split_fp32", tuned)
         extras["split_fp32_single_gate_ms"] = statistics.median(one32[1:])
         extras["fp64_single_gate_ms"] = one
         extras["fp64_single_gate_bootstraps_per_s"] = 1000.0 / one

@@ -311,7 +311,9 @@ void tfhe_gpu_graph_destroy(tfhe_gpu_graph* graph);
 
 /* Time the blind-rotation launch shapes of `form` (tfhe_gpu_set_groups_per_cta)
  * on `count` synthetic ciphertexts with CUDA events, keep the fastest as the
- * context's shape and return it with its time. */
+ * context's shape and return it with its time.  The first candidate (the
+ * automatic shape for split-FP32, 3 for FP64) is kept unless another shape
+ * is more than 2 % faster. */
 tfhe_gpu_status tfhe_gpu_autotune(tfhe_gpu_ctx* ctx, tfhe_gpu_form form, int32_t count,
                                   int32_t* best_shape, float* best_ms);
 
