@@ -42,10 +42,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FLOP_PER_BOOTSTRAP = 162.6e6      # FFT-form algorithmic count, default set
-# DRAM bytes of the blind-rotation kernels, from a full ncu capture of the
-# ring and pair kernels on 1000 gates: every launch reads the 61.9 MB key
-# once (64.4 MB measured with the inputs of 912 gates), and each ciphertext
-# moves 2.5 KB in and 4.5 KB out.
+# DRAM bytes of the blind-rotation kernels, from full ncu captures of the
+# ring and pair kernels: every launch reads the 61.9 MB key once, and each
+# ciphertext moves 2.5 KB in and 4.5 KB out (66.5 MB measured for one
+# 608-gate wave of the batched ring kernel, 66.2 MB by this rule).
 DRAM_KEY_BYTES_PER_LAUNCH = 61.9e6
 DRAM_IO_BYTES_PER_BOOTSTRAP = 2.52e3 + 4.5e3
 BATCH = 4096
@@ -793,7 +793,7 @@ def main():
                          "frac": achieved / peak,
                          "traffic": br_launches * DRAM_KEY_BYTES_PER_LAUNCH + batch * DRAM_IO_BYTES_PER_BOOTSTRAP,
                          "traffic_note": "DRAM bytes of the blind-rotation launches of one step, scaled from "
-                                         "an ncu capture of the same kernels on 1000 gates: key once per "
+                                         "an ncu capture of the same kernels on 700 gates: key once per "
                                          "launch + per-ciphertext I/O",
                          "kernel": " + ".join(blind_rotate_kernels(args.form, eng.get_groups_per_cta(args.form),
                                                                    batch)) + " (blind rotation + extraction)",
@@ -869,18 +869,22 @@ def blind_rotate_kernels(form, shape, batch, l=3):
         return (["k_external_product<double,1,BlindRotate,3,%d>" % l] if shape == 3
                 else ["k_blind_rotate_ring<double,1,4,%d,4,inline>" % l])
     ring = "k_blind_rotate_ring<float,2,%d,%d,4,%s>"
-    batched = "k_blind_rotate_ring<float,2,%d,%d,4,inline,nb%d>"
+    batched = "k_blind_rotate_ring<float,2,4,%d,4,inline,nb%d>" % (l, max(l, 2))
+    pairs = "k_blind_rotate_ring<float,2,6,%d,4,inline,nb2>" % l
     pair = "k_blind_rotate_pair<float,2,%d,%d,4>"
-    nb = max(l, 2)
     if shape == 0:
-        wave = 4 * SMS
+        wave = 6 * SMS
         full, rest = (batch // wave) * wave, batch - (batch // wave) * wave
-        if rest == 0 or rest > 2 * SMS:
-            return [batched % (4, l, nb)]
-        names = [batched % (4, l, nb) + " x %d" % full] if full else []
+        if rest == 0 or rest > 4 * SMS:
+            return [pairs]
+        names = [pairs + " x %d" % full] if full else []
+        if rest > 2 * SMS:
+            return names + [batched + " x %d" % rest]
         return names + [pair % ((rest + SMS - 1) // SMS, l) + " x %d" % rest]
-    if shape in (9, 10):
-        return [batched % (13 - shape, l, nb)]
+    if shape == 9:
+        return [batched]
+    if shape == 10:
+        return [pairs]
     if shape in (11, 12, 13):
         return [pair % (shape - 10, l)]
     if shape in (1, 2, 4):

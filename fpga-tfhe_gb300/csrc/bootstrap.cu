@@ -92,20 +92,25 @@ constexpr int32_t kRoundMagicBits = 0x4B400000;
 
 // round(v / 512) mod 2^32 for |v / 512| < 2^22 (the high key part's product:
 // about 2^18 typical, the exactness limit of FP32 is 2^24): one FMA and one
-// integer add.
-__device__ __forceinline__ uint32_t round_small_u32(float v) {
-    return (uint32_t)(__float_as_int(fmaf(v, 0x1p-9f, kRoundMagic)) - kRoundMagicBits);
+// integer add; both halves of a packed pair at once.
+__device__ __forceinline__ void round_small_pair(cpx<float> z, uint32_t& a0, uint32_t& a1) {
+    const float2 r = __ffma2_rn(pk(z), bc(0x1p-9f), bc(kRoundMagic));
+    a0 = (uint32_t)(__float_as_int(r.x) - kRoundMagicBits);
+    a1 = (uint32_t)(__float_as_int(r.y) - kRoundMagicBits);
 }
 
 // round(v / 512) mod 2^32 for any |v / 512| < 2^53 (the low key part's
 // product, up to about 2^36): the multiple of 2^32 is removed exactly in
-// FP32, and the remainder (|a / 512| <= 2^31) goes through a float -> int32
-// conversion, which does not use the FP64 pipe.  (A remainder of exactly
-// +2^31 saturates one unit short: an error of one unit in the low part.)
-__device__ __forceinline__ uint32_t round_wrap_u32(float v) {
-    const float q = fmaf(v, 0x1p-41f, kRoundMagic) - kRoundMagic;  // rint(v / 2^41)
-    const float a = fmaf(-q, 0x1p41f, v);                             // exact, |a| <= 2^40
-    return (uint32_t)__float2int_rn(a * 0x1p-9f);
+// FP32 (q = rint(v / 2^41), a = v - q 2^41 exact, |a| <= 2^40), and the
+// remainder (|a / 512| <= 2^31) goes through a float -> int32 conversion,
+// which does not use the FP64 pipe.  (A remainder of exactly +2^31
+// saturates one unit short: an error of one unit in the low part.)
+__device__ __forceinline__ void round_wrap_pair(cpx<float> z, uint32_t& a0, uint32_t& a1) {
+    const float2 q = __fadd2_rn(__ffma2_rn(pk(z), bc(0x1p-41f), bc(kRoundMagic)), bc(-kRoundMagic));
+    const float2 a = __ffma2_rn(make_float2(-q.x, -q.y), bc(0x1p41f), pk(z));
+    const float2 sc = __fmul2_rn(a, bc(0x1p-9f));
+    a0 = (uint32_t)__float2int_rn(sc.x);
+    a1 = (uint32_t)__float2int_rn(sc.y);
 }
 
 // Gadget digit of u at `decal` as a transform input: ((u >> decal) & mask) -
@@ -135,30 +140,12 @@ __device__ __forceinline__ cpx<R> digit_pair(uint32_t u0, uint32_t u1, int decal
     }
 }
 
-// round_small_u32 / round_wrap_u32 on both halves of a packed pair.
-__device__ __forceinline__ void round_small_pair(cpx<float> z, uint32_t& a0, uint32_t& a1) {
-    const float2 r = __ffma2_rn(pk(z), bc(0x1p-9f), bc(kRoundMagic));
-    a0 = (uint32_t)(__float_as_int(r.x) - kRoundMagicBits);
-    a1 = (uint32_t)(__float_as_int(r.y) - kRoundMagicBits);
-}
-__device__ __forceinline__ void round_wrap_pair(cpx<float> z, uint32_t& a0, uint32_t& a1) {
-    const float2 q = __fadd2_rn(__ffma2_rn(pk(z), bc(0x1p-41f), bc(kRoundMagic)), bc(-kRoundMagic));
-    const float2 a = __ffma2_rn(make_float2(-q.x, -q.y), bc(0x1p41f), pk(z));
-    const float2 sc = __fmul2_rn(a, bc(0x1p-9f));
-    a0 = (uint32_t)__float2int_rn(sc.x);
-    a1 = (uint32_t)__float2int_rn(sc.y);
-}
-
 template <typename R>
 __device__ __forceinline__ int64_t to_int(R v);
 template <>
 __device__ __forceinline__ int64_t to_int<double>(double v) {
     // reference semantics: int64_t(double) truncates (TorusPolynomial_fft.cpp:40)
     return __double2ll_rz(v);
-}
-template <>
-__device__ __forceinline__ int64_t to_int<float>(float v) {
-    return __float2ll_rn(v);
 }
 
 // ----------------------------------------------------------------------
@@ -276,9 +263,36 @@ __device__ __forceinline__ void mac_row(cpx<R> (&out)[2][PARTS][8], const cpx<R>
         }
 }
 
+// Levels lev0 .. lev0 + NBK - 1 of input polynomial jp: digits, NBK forward
+// transforms run together, and their key rows multiply-accumulated.
+template <int NBK, typename R, int PARTS, int NB, typename Keys>
+__device__ __forceinline__ void forward_levels(const StepCtx<R, PARTS, NB>& S, Keys& keys,
+                                               cpx<R> (&out)[2][PARTS][8], const uint32_t (&r0)[8],
+                                               const uint32_t (&r1)[8], int p0, int lev0, uint32_t mask,
+                                               int halfBg) {
+    const int t = S.t;
+    cpx<R> v[NBK][8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+#pragma unroll
+        for (int b = 0; b < NBK; ++b) {
+            const int decal = 32 - (lev0 + b + 1) * S.Bgbit;
+            v[b][r] = digit_pair<R>(r0[r], r1[r], decal, mask, halfBg);
+        }
+    }
+    fft512_forward_tw_multi<NBK>(v, *reinterpret_cast<const FftScratch<R>(*)[NBK]>(S.s), S.tw, S.ix, t,
+                                 S.bar_id);
+#pragma unroll
+    for (int b = 0; b < NBK; ++b) {
+        const int p = p0 + lev0 + b;
+        mac_row<R, PARTS, Keys::kShared>(out, v[b], keys.acquire(p), t);
+        keys.release(p);
+    }
+}
+
 template <typename R, int PARTS, bool ROT, int L, int FB, int IB, int NB, typename Keys>
 __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& keys, int a) {
-    static_assert(L % FB == 0 && PARTS % IB == 0 && FB <= NB && IB <= NB, "batch sizes");
+    static_assert(PARTS % IB == 0 && FB <= NB && IB <= NB, "batch sizes");
     const int t = S.t;
     const int halfBg = 1 << (S.Bgbit - 1);
     const uint32_t mask = (1u << S.Bgbit) - 1;
@@ -309,26 +323,12 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
             r0[r] += S.offset;
             r1[r] += S.offset;
         }
+        // blocks of FB levels, then the remaining L % FB together
 #pragma unroll
-        for (int lev0 = 0; lev0 < L; lev0 += FB) {
-            cpx<R> v[FB][8];
-#pragma unroll
-            for (int r = 0; r < 8; ++r) {
-#pragma unroll
-                for (int b = 0; b < FB; ++b) {
-                    const int decal = 32 - (lev0 + b + 1) * S.Bgbit;
-                    v[b][r] = digit_pair<R>(r0[r], r1[r], decal, mask, halfBg);
-                }
-            }
-            fft512_forward_tw_multi<FB>(v, *reinterpret_cast<const FftScratch<R>(*)[FB]>(S.s), S.tw, S.ix, t,
-                                        S.bar_id);
-#pragma unroll
-            for (int b = 0; b < FB; ++b) {
-                const int p = jp * L + lev0 + b;
-                mac_row<R, PARTS, Keys::kShared>(out, v[b], keys.acquire(p), t);
-                keys.release(p);
-            }
-        }
+        for (int lev0 = 0; lev0 + FB <= L; lev0 += FB)
+            forward_levels<FB>(S, keys, out, r0, r1, jp * L, lev0, mask, halfBg);
+        if constexpr (L % FB != 0)
+            forward_levels<L % FB>(S, keys, out, r0, r1, jp * L, L - L % FB, mask, halfBg);
     }
 
     // back to the coefficient domain (j unrolled: out[j] must stay in registers)
@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(64 * GROUPS, 1) k_external_product(KParams kp,
     constexpr int NB = L > PARTS ? L : PARTS;
     using Ctx = StepCtx<R, PARTS, NB>;
     using Plan = SmemPlan<R, NB>;
-    extern __shared__ __align__(16) char smem[];
+    extern __shared__ __align__(128) char smem[];
     cpx<R>* tables = reinterpret_cast<cpx<R>*>(smem);
     load_hot_tables<R>(tables, T);
     __syncthreads();
@@ -809,7 +809,7 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
             continue;
         }
         if constexpr (NB == 1) ep_step_lean<R, PARTS, L>(St, keys, ai);
-        else ep_step<R, PARTS, true, L, L, PARTS, NB>(St, keys, ai);
+        else ep_step<R, PARTS, true, L, (NB < L ? NB : L), PARTS, NB>(St, keys, ai);
     }
     if (keys.producer) keys.drain();
     if (a.acc_out) {
@@ -1060,7 +1060,7 @@ constexpr size_t kConvTableBytes = kTabSize * sizeof(cpx<double>);
 template <int FORM>
 __global__ void __launch_bounds__(256) k_tgsw_to_fft(Tables T, const int32_t* __restrict__ in,
                                                      void* out, int npoly, int split) {
-    extern __shared__ __align__(16) char smem[];
+    extern __shared__ __align__(128) char smem[];
     cpx<double>* tables = reinterpret_cast<cpx<double>*>(smem);
     load_tables<double>(tables, T);
     __syncthreads();
@@ -1106,7 +1106,7 @@ __global__ void __launch_bounds__(256) k_tgsw_to_fft(Tables T, const int32_t* __
 // engine FP64 layout -> integer coefficients (rounded to nearest)
 __global__ void __launch_bounds__(256) k_fft64_to_tgsw(Tables T, const void* in,
                                                        int32_t* __restrict__ out, int npoly) {
-    extern __shared__ __align__(16) char smem[];
+    extern __shared__ __align__(128) char smem[];
     cpx<double>* tables = reinterpret_cast<cpx<double>*>(smem);
     load_tables<double>(tables, T);
     __syncthreads();
@@ -1149,7 +1149,7 @@ __device__ __forceinline__ void engine_to_ref_index(int m, int* ref, bool* conj)
 __global__ void __launch_bounds__(256) k_poly_to_lagrange(Tables T, const int32_t* __restrict__ in,
                                                           double* __restrict__ out, int npoly,
                                                           double scale) {
-    extern __shared__ __align__(16) char smem[];
+    extern __shared__ __align__(128) char smem[];
     cpx<double>* tables = reinterpret_cast<cpx<double>*>(smem);
     load_tables<double>(tables, T);
     __syncthreads();
@@ -1179,7 +1179,7 @@ __global__ void __launch_bounds__(256) k_poly_to_lagrange(Tables T, const int32_
 // Torus32 coefficients, truncating like TorusPolynomial_fft.cpp:39-41.
 __global__ void __launch_bounds__(256) k_lagrange_to_torus(Tables T, const double* __restrict__ in,
                                                            int32_t* __restrict__ out, int npoly) {
-    extern __shared__ __align__(16) char smem[];
+    extern __shared__ __align__(128) char smem[];
     cpx<double>* tables = reinterpret_cast<cpx<double>*>(smem);
     load_tables<double>(tables, T);
     __syncthreads();
@@ -1406,30 +1406,39 @@ cudaError_t launch_pair_fp32(const DevParams& P, const Tables& T, const EpArgs& 
     return launch_pair_t<float, 2, 3, L, 4>(P, T, a, st);
 }
 
-// Automatic shape of a split-FP32 blind rotation over `count` ciphertexts:
-// whole waves of four ciphertexts per SM on the shared-ring kernel with a
-// step's transforms run together; a remainder of at most two per SM on the
-// pair kernel (two halves per ciphertext: measured 2.6 ms for one and 3.3 ms
-// for two per SM against 4.5 ms for a ring wave of any fill); a larger
-// remainder as one more ring wave (4.5 ms for three per SM, the pair kernel
-// 5.1 ms).
+// Batched ring kernels: 4 per CTA with a step's l forward transforms run
+// together (250 registers, 8 warps per SM), or 6 per CTA with transforms two
+// at a time (168 registers, 12 warps per SM).
 template <int L>
 cudaError_t launch_ring_batched(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
     return launch_ring_t<float, 2, 4, L, true, 4, (L > 2 ? L : 2)>(P, T, a, st);
 }
+template <int L>
+cudaError_t launch_ring_pairs(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
+    return launch_ring_t<float, 2, 6, L, true, 4, 2>(P, T, a, st);
+}
 
+// Automatic shape of a split-FP32 blind rotation over `count` ciphertexts.
+// Measured per launch (default set): a wave of 6 per SM on
+// launch_ring_pairs 6.6 ms (138K gates/s), of 4 per SM on
+// launch_ring_batched 4.6 ms (132K/s), whatever the fill of the wave; the
+// pair kernel 2.6 ms at 1 per SM, 3.3 ms at 2, 5.1 ms at 3.  So: whole waves
+// of 6 per SM; a remainder of at most 2 per SM on the pair kernel, of at
+// most 4 per SM as one launch_ring_batched wave, else one more 6-per-SM
+// wave.
 template <int L>
 cudaError_t launch_auto_fp32(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
-    const int wave = 4 * kSmCount;
+    const int wave = 6 * kSmCount;
     const int full = (a.count / wave) * wave;
     const int rest = a.count - full;
-    if (rest == 0 || rest > 2 * kSmCount) return launch_ring_batched<L>(P, T, a, st);
+    if (rest == 0 || rest > 4 * kSmCount) return launch_ring_pairs<L>(P, T, a, st);
     if (full) {
-        cudaError_t e = launch_ring_batched<L>(P, T, slice_blind_rotate(P, a, 0, full), st);
+        cudaError_t e = launch_ring_pairs<L>(P, T, slice_blind_rotate(P, a, 0, full), st);
         if (e != cudaSuccess) return e;
     }
-    const int per_cta = (rest + kSmCount - 1) / kSmCount;
-    return launch_pair_fp32<L>(P, T, slice_blind_rotate(P, a, full, rest), per_cta, st);
+    const EpArgs tail = slice_blind_rotate(P, a, full, rest);
+    if (rest > 2 * kSmCount) return launch_ring_batched<L>(P, T, tail, st);
+    return launch_pair_fp32<L>(P, T, tail, (rest + kSmCount - 1) / kSmCount, st);
 }
 
 // FP64: ~250 registers per thread and 2 x L exchange buffers of 9 KB per
@@ -1453,11 +1462,12 @@ cudaError_t launch_ep_l(const DevParams& P, Form f, EpMode mode, const Tables& T
         if (groups == 0) return launch_auto_fp32<L>(P, T, a, st);
         // 1, 2, 4: L2-direct key reads; 5: shared ring fed by a producer
         // warp; 6, 7, 8: shared ring fed in line by one consumer thread;
-        // 9, 10: shared ring with a step's transforms run together, 4 or 3
-        // groups; 11, 12, 13: pair kernel with 1, 2, 3 ciphertexts per CTA
+        // 9: shared ring, 4 per CTA, a step's l forward transforms run
+        // together; 10: shared ring, 6 per CTA, transforms two at a time;
+        // 11, 12, 13: pair kernel with 1, 2, 3 ciphertexts per CTA
         if (groups >= 11 && groups <= 13) return launch_pair_fp32<L>(P, T, a, groups - 10, st);
         if (groups == 9) return launch_ring_batched<L>(P, T, a, st);
-        if (groups == 10) return launch_ring_t<float, 2, 3, L, true, 4, (L > 2 ? L : 2)>(P, T, a, st);
+        if (groups == 10) return launch_ring_pairs<L>(P, T, a, st);
         if (groups == 1) return launch_ep_t<float, 2, kEpBlindRotate, 1, L>(P, T, a, st);
         if (groups == 2) return launch_ep_t<float, 2, kEpBlindRotate, 2, L>(P, T, a, st);
         if (groups == 4) return launch_ep_t<float, 2, kEpBlindRotate, 4, L>(P, T, a, st);

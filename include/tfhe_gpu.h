@@ -101,16 +101,17 @@ size_t tfhe_gpu_tgsw_fft_bytes(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form);
 size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
 
 /* Launch shape of the blind-rotation kernel of `form`.  split-FP32:
- *   0 = automatic: whole waves of 4 ciphertexts per SM on shape 9, a
- *       remainder of at most 2 per SM on the pair kernel, a larger one as
- *       one more shape-9 wave;
+ *   0 = automatic: whole waves of 6 ciphertexts per SM on shape 10; a
+ *       remainder of at most 2 per SM on the pair kernel, of at most 4 per
+ *       SM as one shape-9 wave, else one more shape-10 wave;
  *   1, 2, 4 = ciphertexts (64 threads each) per CTA, key rows read from L2
  *       by every ciphertext;
  *   5 = 5 per CTA, key rows streamed once per CTA into a shared-memory ring
  *       by a producer warp;
  *   6, 7, 8 = that many per CTA, the same ring fed by one consumer thread;
- *   9, 10 = 4 or 3 per CTA on the same ring, each step's l forward and
- *       2 inverse transforms run together (about 250 registers a thread);
+ *   9 = 4 per CTA on the same ring, each step's l forward and 2 inverse
+ *       transforms run together (about 250 registers a thread);
+ *   10 = 6 per CTA on the same ring, transforms two at a time;
  *   11, 12, 13 = pair kernel: two 64-thread halves per ciphertext (about
  *       half the latency), 1, 2, 3 ciphertexts per CTA, shared ring.
  * FP64: 3 (L2) or 4 (ring, in line).  Engine tuning knob, no counterpart in

@@ -260,14 +260,16 @@ def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, grou
     assert np.abs(d).max() <= PHASE_TOL
 
 
-def test_auto_shape_full_wave_and_tail(pkg, oracle, keys, torch_cuda, P, inputs):
-    """The automatic split-FP32 shape on one full wave (4 per SM on the
-    batched ring kernel) plus a tail of 40 on the pair kernel: every output
-    decrypts to the truth and ciphertexts from both launches match the
-    oracle's phases."""
+@pytest.mark.parametrize("tail", [40, 400])
+def test_auto_shape_full_wave_and_tail(pkg, oracle, keys, torch_cuda, P, inputs, tail):
+    """The automatic split-FP32 shape on one full wave (6 per SM on the ring
+    kernel with transforms two at a time) plus a tail on the pair kernel (40)
+    or on the 4-per-SM batched ring kernel (400): every output decrypts to
+    the truth and ciphertexts from both launches match the oracle's
+    phases."""
     torch = torch_cuda
     a, b, ca, cb = inputs
-    count = 4 * 152 + 40
+    count = 6 * 152 + tail
     reps = (count + len(a) - 1) // len(a)
     a, b = np.tile(a, reps)[:count], np.tile(b, reps)[:count]
     ca, cb = np.tile(ca, (reps, 1))[:count], np.tile(cb, (reps, 1))[:count]
@@ -288,7 +290,7 @@ def test_auto_shape_full_wave_and_tail(pkg, oracle, keys, torch_cuda, P, inputs)
     names = sorted(pyoracle.GATES, key=lambda g: pyoracle.GATES[g])
     truth = np.array([pyoracle.GATE_FN[names[g]](x, y) for g, x, y in zip(gates, a, b)])
     assert (oracle.decrypt_bits(P, got, keys["lwe"]) == truth).all()
-    idx = np.array([0, 1, 607, 608, 609, count - 1])
+    idx = np.array([0, 1, 911, 912, 913, count - 1])
     ref = oracle.boots_gate_batch(P, keys["bk_fft"], keys["ks"], gates[idx], ca[idx], cb[idx])
     d = wrap_diff(oracle.phases(got[idx], keys["lwe"], P.n), oracle.phases(ref, keys["lwe"], P.n))
     assert np.abs(d).max() <= PHASE_TOL
@@ -366,14 +368,14 @@ def test_stress_set_noise_band(pkg, torch_cuda):
         e.close()
 
 
-@pytest.mark.parametrize("groups,count", [(0, 8), (6, 6), (9, 9), (13, 5), (5, 5)])
+@pytest.mark.parametrize("groups,count", [(0, 8), (6, 6), (9, 9), (10, 7), (13, 5), (5, 5)])
 def test_bounded_waits_report_timeout(pkg, oracle, keys, torch_cuda, P, inputs, groups, count):
     """The device-side failure path without a fault: a blind rotation whose
     key-row stream never starts (a flag the producer honours) makes every
     consumer's bounded wait run out; the kernel ends within a few seconds,
     the host gets TFHE_GPU_TIMEOUT, and the same context then bootstraps
-    correctly.  Shapes: automatic (pair kernel), ring in line, batched ring,
-    pair, ring with a producer warp."""
+    correctly.  Shapes: automatic (pair kernel), ring in line, the two
+    batched rings, pair, ring with a producer warp."""
     import time
     torch = torch_cuda
     e = pkg.Engine(pkg.default_params())
@@ -408,12 +410,12 @@ def test_l2_shape_has_no_waits(pkg, keys, torch_cuda):
         e.close()
 
 
-@pytest.mark.parametrize("count", [304, 305, 608, 609, 912, 913])
+@pytest.mark.parametrize("count", [304, 305, 608, 609, 912, 913, 1216, 1217, 1520, 1521])
 def test_auto_shape_boundaries(pkg, engine, oracle, keys, torch_cuda, P, count):
-    """Batch sizes on both sides of the automatic shape's boundaries (pair
-    only up to 2 per SM; a partial ring wave above that; ring waves of 4 per
-    SM; ring + pair tail; ring + a partial ring wave): every output decrypts
-    to the truth."""
+    """Batch sizes on both sides of the automatic shape's boundaries: pair
+    kernel only up to 2 per SM; one 4-per-SM wave up to 4 per SM; 6-per-SM
+    waves; a wave plus a pair tail, plus a 4-per-SM tail, plus a partial
+    6-per-SM wave: every output decrypts to the truth."""
     torch = torch_cuda
     rng = np.random.default_rng(97 + count)
     a = rng.integers(0, 2, count)
