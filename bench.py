@@ -788,7 +788,9 @@ def main():
             "decrypt_ok": ok,
             "e2e": {"value": e2e_value, "unit": "bootstraps/s",
                     "h2d_bytes_per_step": 2 * lwe_bytes + batch * 4, "d2h_bytes_per_step": lwe_bytes},
-            "gpu_launches": (graph.kernels if graph is not None else 3) * args.steps,
+            # eager: combine + per blind-rotation launch one key-switch launch
+            # (a split blind rotation has its key switch split the same way)
+            "gpu_launches": (graph.kernels if graph is not None else 1 + 2 * br_launches) * args.steps,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak,
                          "traffic": br_launches * DRAM_KEY_BYTES_PER_LAUNCH + batch * DRAM_IO_BYTES_PER_BOOTSTRAP,

@@ -1581,6 +1581,16 @@ cudaError_t launch_engine64_to_lagrange_ref(const void* eng, double* ref, int np
     return cudaGetLastError();
 }
 
+int blind_rotate_tail_start(Form f, int groups, int count) {
+    // launch_auto_fp32's split: whole 6-per-SM waves, then a remainder of
+    // at most 4 per SM that runs as its own launch on part of the SMs
+    if (f != kFormSplitFp32 || groups != 0) return 0;
+    const int wave = 6 * kSmCount;
+    const int full = (count / wave) * wave;
+    const int rest = count - full;
+    return full > 0 && rest > 0 && rest <= 4 * kSmCount ? full : 0;
+}
+
 cudaError_t launch_external_product(const DevParams& P, Form f, EpMode mode, const Tables& T,
                                     const EpArgs& a, int groups, cudaStream_t st) {
     switch (P.l) {

@@ -153,8 +153,26 @@ tfhe_gpu_status run_gates_in(tfhe_gpu_ctx* ctx, const int32_t* gates, int32_t un
                              int32_t form, int32_t* x, int32_t* u, cudaStream_t st) {
     CK(ctx, launch_gate_combine(ctx->dp, gates, uniform_gate, ca, cb, x, count, st));
     const int32_t mu = tfhe_client_mod_switch_to_torus32(1, 8);
-    RET(run_bootstrap_woks(ctx, x, mu, u, count, form, st));
-    CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, u, out, count, st));
+    const int split = blind_rotate_tail_start((Form)form, ctx->groups_per_cta[form], count);
+    if (split == 0) {
+        RET(run_bootstrap_woks(ctx, x, mu, u, count, form, st));
+        CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, u, out, count, st));
+        return TFHE_GPU_OK;
+    }
+    // The remainder wave of the blind rotation occupies only part of the
+    // SMs: issue it right after the full waves, and the full waves' key
+    // switch on the side stream, which fills the idle SMs meanwhile.
+    const int n = ctx->P.n, nk = ctx->P.k * ctx->P.N;
+    RET(run_bootstrap_woks(ctx, x, mu, u, split, form, st));
+    CK(ctx, cudaEventRecord(ctx->ev_fork, st));
+    RET(run_bootstrap_woks(ctx, x + (size_t)split * (n + 1), mu, u + (size_t)split * (nk + 1), count - split,
+                           form, st));
+    CK(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+    CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, u, out, split, ctx->side));
+    CK(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
+    CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, u + (size_t)split * (nk + 1),
+                             out + (size_t)split * (n + 1), count - split, st));
+    CK(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
     return TFHE_GPU_OK;
 }
 
@@ -221,7 +239,10 @@ tfhe_gpu_status tfhe_gpu_create(const tfhe_params* params, int32_t device, tfhe_
         return s;
     };
     if (cudaSetDevice(device) != cudaSuccess) return bail(TFHE_GPU_DEVICE_ERROR);
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
         return bail(TFHE_GPU_DEVICE_ERROR);
     const int nt = 2 * twiddle_table_entries();
     std::vector<double> h64(nt);
@@ -247,6 +268,7 @@ void tfhe_gpu_destroy(tfhe_gpu_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
     for (int f = 0; f < kNumForms; ++f)
         if (ctx->d_bk[f]) cudaFree(ctx->d_bk[f]);
     if (ctx->d_ks) cudaFree(ctx->d_ks);
@@ -254,6 +276,9 @@ void tfhe_gpu_destroy(tfhe_gpu_ctx* ctx) {
         if (ctx->d_scratch[s]) cudaFree(ctx->d_scratch[s]);
     if (ctx->d_tables) cudaFree(ctx->d_tables);
     if (ctx->d_err) cudaFree(ctx->d_err);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

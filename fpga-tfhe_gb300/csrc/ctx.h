@@ -18,6 +18,10 @@ struct tfhe_gpu_ctx {
     DevParams dp;
     int device = 0;
     cudaStream_t stream = nullptr;
+    // fork/join of a gate batch: the key switch of the full blind-rotation
+    // waves runs on `side` while the remainder wave leaves SMs idle
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     void* d_tables = nullptr;  // transform tables: FP64 copy then FP32 copy
     Tables tables{};
     void* d_bk[kNumForms] = {nullptr, nullptr};

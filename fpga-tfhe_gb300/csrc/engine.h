@@ -115,6 +115,11 @@ cudaError_t launch_lagrange_addmul(const double* a, const double* b,
                                    double* acc, int npoly, int half,
                                    cudaStream_t st);
 
+// Where the automatic split-FP32 blind rotation of `count` ciphertexts
+// starts its remainder launch (one that leaves SMs idle), or 0 when it is a
+// single launch or another shape is set.
+int blind_rotate_tail_start(Form f, int groups, int count);
+
 // Key switching: in (count x (kN+1)) -> out (count x (n+1)); ks rows are
 // `row_stride` int32 apart, layout [kN][t][base][row_stride].
 cudaError_t launch_keyswitch(const DevParams& P, const int32_t* ks,
