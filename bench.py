@@ -795,7 +795,7 @@ def main():
                          "frac": achieved / peak,
                          "traffic": br_launches * DRAM_KEY_BYTES_PER_LAUNCH + batch * DRAM_IO_BYTES_PER_BOOTSTRAP,
                          "traffic_note": "DRAM bytes of the blind-rotation launches of one step, scaled from "
-                                         "an ncu capture of the same kernels on 700 gates: key once per "
+                                         "ncu captures of the same kernels (1360 gates): key once per "
                                          "launch + per-ciphertext I/O",
                          "kernel": " + ".join(blind_rotate_kernels(args.form, eng.get_groups_per_cta(args.form),
                                                                    batch)) + " (blind rotation + extraction)",
