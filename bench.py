@@ -874,6 +874,7 @@ def blind_rotate_kernels(form, shape, batch, l=3):
     batched = "k_blind_rotate_ring<float,2,4,%d,4,inline,nb%d>" % (l, max(l, 2))
     pairs = "k_blind_rotate_ring<float,2,6,%d,4,inline,nb2>" % l
     pair = "k_blind_rotate_pair<float,2,%d,%d,4>"
+    spread = "k_blind_rotate_spread<%d>" % l
     if shape == 0:
         wave = 6 * SMS
         full, rest = (batch // wave) * wave, batch - (batch // wave) * wave
@@ -882,7 +883,11 @@ def blind_rotate_kernels(form, shape, batch, l=3):
         names = [pairs + " x %d" % full] if full else []
         if rest > 2 * SMS:
             return names + [batched + " x %d" % rest]
-        return names + [pair % ((rest + SMS - 1) // SMS, l) + " x %d" % rest]
+        if rest > SMS:
+            return names + [pair % (2, l) + " x %d" % rest]
+        return names + [spread + " x %d" % rest]
+    if shape == 14:
+        return [spread]
     if shape == 9:
         return [batched]
     if shape == 10:

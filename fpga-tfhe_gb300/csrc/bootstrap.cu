@@ -825,6 +825,151 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
 }
 
 // ----------------------------------------------------------------------
+// Blind rotation with one ciphertext over 2l groups (lowest latency).
+//
+// Group g = (jp, lev) = (g / l, g % l) decomposes input polynomial jp at
+// level lev, runs that one forward transform, multiplies it with its key
+// row (read from L2; the next step's row is prefetched into L1) and writes
+// the partial products of both outputs and both key parts to shared memory.
+// After a CTA barrier, group (j, pt) = (g / 2, g % 2) for g < 4 sums the 2l
+// partials of output j, part pt in a fixed order, transforms back, rounds,
+// and adds its part into the accumulator with integer shared-memory atomics
+// (exact mod 2^32 in any order, so the result does not depend on timing).
+// A step's critical path is one forward and one inverse transform instead
+// of the pair kernel's l forward and PARTS inverse ones.  Split-FP32 only.
+// ----------------------------------------------------------------------
+template <int L>
+struct SpreadPlan {
+    static constexpr int kGroups = 2 * L;
+    static constexpr size_t tables = kHotSize * sizeof(cpx<float>);
+    static constexpr size_t acc_off = tables;
+    static constexpr size_t part_off = acc_off + 2 * kN * sizeof(int32_t);
+    static constexpr size_t part = 4 * kHalf * sizeof(cpx<float>);  // [j * 2 + pt][q][t]
+    static constexpr size_t scratch_off = part_off + kGroups * part;
+    static constexpr size_t scratch = 2 * kScratchStride * sizeof(cpx<float>);
+    static constexpr size_t total = scratch_off + kGroups * scratch;
+};
+
+template <int L>
+__global__ void __launch_bounds__(128 * L, 1) k_blind_rotate_spread(KParams kp, Tables T, EpArgs a) {
+    using Plan = SpreadPlan<L>;
+    constexpr int kRowElems = 2 * 2 * kHalf;  // complex values per key row
+    extern __shared__ __align__(128) char smem[];
+    cpx<float>* tables = reinterpret_cast<cpx<float>*>(smem);
+    int32_t* acc = reinterpret_cast<int32_t*>(smem + Plan::acc_off);
+    cpx<float>* part = reinterpret_cast<cpx<float>*>(smem + Plan::part_off);
+    const int c = blockIdx.x;
+    const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
+    const int jp = g / L, lev = g - jp * L;
+    const int n = kp.n;
+    load_hot_tables<float>(tables, T);
+    if (a.acc_in) {
+        const int32_t* src = a.acc_in + (size_t)c * 2 * kN;
+        for (int i = threadIdx.x; i < 2 * kN; i += blockDim.x) acc[i] = src[i];
+    } else {
+        const int32_t* xs = a.x + (size_t)c * (n + 1);
+        const int barb = mod_switch_2n(xs[n]);
+        for (int i = threadIdx.x; i < kN; i += blockDim.x) {
+            acc[i] = 0;
+            acc[kN + i] = test_vector_coef(a, c, barb, i);
+        }
+    }
+    __syncthreads();
+
+    const FftTwiddles<float> tw = hot_twiddles<float>(tables);
+    const FftIdx ix = make_fft_idx(t);
+    const FftScratch<float> sc = scratch_at<float>(smem + Plan::scratch_off + (size_t)g * Plan::scratch);
+    const int bar_id = 1 + g;
+    const int halfBg = 1 << (kp.Bgbit - 1);
+    const uint32_t mask = (1u << kp.Bgbit) - 1;
+    const int decal = 32 - (lev + 1) * kp.Bgbit;
+    const cpx<float>* gsw = reinterpret_cast<const cpx<float>*>(a.gsw);
+    const size_t step_elems = (size_t)2 * L * kRowElems;
+    const int32_t* bara = a.bara ? a.bara + (size_t)c * n : nullptr;
+    const int32_t* xs = a.x ? a.x + (size_t)c * (n + 1) : nullptr;
+    int a_next = bara ? bara[0] : mod_switch_2n(xs[0]);
+    {  // this group's first key row into L1
+        const char* row = reinterpret_cast<const char*>(gsw + (size_t)g * kRowElems);
+        for (int ln = t; ln < kRowElems * (int)sizeof(cpx<float>) / 128; ln += 64)
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(row + (size_t)ln * 128));
+    }
+#pragma unroll 1
+    for (int i = 0; i < n; ++i) {
+        const int ai = a_next;
+        if (i + 1 < n) a_next = bara ? bara[i + 1] : mod_switch_2n(xs[i + 1]);
+        if (ai == 0) continue;  // tfhe_blindRotate_FFT.cpp:114 (uniform over the CTA)
+        const cpx<float>* row = gsw + (size_t)i * step_elems + (size_t)g * kRowElems;
+        // forward: polynomial jp of (X^a - 1) acc at level lev
+        cpx<float> v[8];
+        {
+            const int32_t* src = acc + jp * kN;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int x0 = t + 64 * r;
+                const uint32_t u0 = (uint32_t)rot_coef(src, x0, ai) - (uint32_t)src[x0] + kp.offset;
+                const uint32_t u1 =
+                    (uint32_t)rot_coef(src, x0 + kHalf, ai) - (uint32_t)src[x0 + kHalf] + kp.offset;
+                v[r] = digit_pair<float>(u0, u1, decal, mask, halfBg);
+            }
+        }
+        fft512_forward_tw(v, sc, tw, ix, t, bar_id);
+        cpx<float> out[2][2][8];
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int pt = 0; pt < 2; ++pt)
+#pragma unroll
+                for (int q = 0; q < 8; ++q) out[j][pt][q] = {0.f, 0.f};
+        mac_row<float, 2, false>(out, v, row, t);
+        if (i + 1 < n) {  // next step's row into L1 while the others finish
+            const char* nrow = reinterpret_cast<const char*>(row + step_elems);
+            for (int ln = t; ln < kRowElems * (int)sizeof(cpx<float>) / 128; ln += 64)
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(nrow + (size_t)ln * 128));
+        }
+        cpx<float>* mine = part + (size_t)g * 4 * kHalf;
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int pt = 0; pt < 2; ++pt)
+#pragma unroll
+                for (int q = 0; q < 8; ++q) mine[((j * 2 + pt) * 8 + q) * 64 + t] = out[j][pt][q];
+        __syncthreads();  // every partial written, every read of acc done
+        if (g < 4) {
+            const int j = g >> 1, pt = g & 1;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = part[((j * 2 + pt) * 8 + q) * 64 + t];
+#pragma unroll
+            for (int gg = 1; gg < 2 * L; ++gg)
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    v[q] = cadd(v[q], part[(size_t)gg * 4 * kHalf + ((j * 2 + pt) * 8 + q) * 64 + t]);
+            fft512_inverse_tw(v, sc, tw, ix, t, bar_id);
+            uint32_t c0[8] = {}, c1[8] = {};  // the low part adds into them
+            round_part<float, 2>(v, pt, kp.split, c0, c1);
+            int32_t* dst = acc + j * kN;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int x0 = t + 64 * q;
+                atomicAdd(reinterpret_cast<unsigned*>(dst + x0), c0[q]);
+                atomicAdd(reinterpret_cast<unsigned*>(dst + x0 + kHalf), c1[q]);
+            }
+        }
+        __syncthreads();  // the accumulator is updated before the next step reads it
+    }
+    if (a.acc_out) {
+        int32_t* dst = a.acc_out + (size_t)c * 2 * kN;
+        for (int i = threadIdx.x; i < 2 * kN; i += blockDim.x) dst[i] = acc[i];
+    }
+    if (a.lwe_out) {
+        // tLweExtractLweSample: a'_0 = a_0, a'_j = -a_{N-j}, b' = b_0
+        int32_t* dst = a.lwe_out + (size_t)c * (kN + 1);
+        for (int i = threadIdx.x; i < kN; i += blockDim.x)
+            dst[i] = i == 0 ? acc[0] : (int32_t)(0u - (uint32_t)acc[kN - i]);
+        if (threadIdx.x == 0) dst[kN] = acc[kN];
+    }
+}
+
+// ----------------------------------------------------------------------
 // Blind rotation with two 64-thread halves per ciphertext (low latency).
 //
 // Half h of a ciphertext decomposes and transforms input polynomial h (rows
@@ -1395,6 +1540,18 @@ cudaError_t launch_pair_t(const DevParams& P, const Tables& T, const EpArgs& a, 
     return cudaGetLastError();
 }
 
+template <int L>
+cudaError_t launch_spread(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
+    if (a.count <= 0) return cudaSuccess;
+    const KParams kp = make_kparams(P);
+    using Plan = SpreadPlan<L>;
+    auto kern = k_blind_rotate_spread<L>;
+    cudaError_t e = set_smem(kern, Plan::total);
+    if (e != cudaSuccess) return e;
+    kern<<<a.count, 128 * L, Plan::total, st>>>(kp, T, a);
+    return cudaGetLastError();
+}
+
 // split-FP32 pair kernel with `per_cta` (1..3) ciphertexts per CTA
 template <int L>
 cudaError_t launch_pair_fp32(const DevParams& P, const Tables& T, const EpArgs& a, int per_cta,
@@ -1422,10 +1579,11 @@ cudaError_t launch_ring_pairs(const DevParams& P, const Tables& T, const EpArgs&
 // Measured per launch (default set): a wave of 6 per SM on
 // launch_ring_pairs 6.6 ms (138K gates/s), of 4 per SM on
 // launch_ring_batched 4.6 ms (132K/s), whatever the fill of the wave; the
-// pair kernel 2.6 ms at 1 per SM, 3.3 ms at 2, 5.1 ms at 3.  So: whole waves
-// of 6 per SM; a remainder of at most 2 per SM on the pair kernel, of at
-// most 4 per SM as one launch_ring_batched wave, else one more 6-per-SM
-// wave.
+// spread kernel 2.1 ms at 1 per SM (4.2 ms for two waves); the pair kernel
+// 2.6 ms at 1 per SM, 3.3 ms at 2, 5.1 ms at 3.  So: whole waves of 6 per
+// SM; a remainder of at most 1 per SM on the spread kernel, of 2 per SM on
+// the pair kernel, of at most 4 per SM as one launch_ring_batched wave, else
+// one more 6-per-SM wave.
 template <int L>
 cudaError_t launch_auto_fp32(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
     const int wave = 6 * kSmCount;
@@ -1438,7 +1596,8 @@ cudaError_t launch_auto_fp32(const DevParams& P, const Tables& T, const EpArgs& 
     }
     const EpArgs tail = slice_blind_rotate(P, a, full, rest);
     if (rest > 2 * kSmCount) return launch_ring_batched<L>(P, T, tail, st);
-    return launch_pair_fp32<L>(P, T, tail, (rest + kSmCount - 1) / kSmCount, st);
+    if (rest > kSmCount) return launch_pair_fp32<L>(P, T, tail, 2, st);
+    return launch_spread<L>(P, T, tail, st);
 }
 
 // FP64: ~250 registers per thread and 2 x L exchange buffers of 9 KB per
@@ -1468,6 +1627,7 @@ cudaError_t launch_ep_l(const DevParams& P, Form f, EpMode mode, const Tables& T
         if (groups >= 11 && groups <= 13) return launch_pair_fp32<L>(P, T, a, groups - 10, st);
         if (groups == 9) return launch_ring_batched<L>(P, T, a, st);
         if (groups == 10) return launch_ring_pairs<L>(P, T, a, st);
+        if (groups == 14) return launch_spread<L>(P, T, a, st);
         if (groups == 1) return launch_ep_t<float, 2, kEpBlindRotate, 1, L>(P, T, a, st);
         if (groups == 2) return launch_ep_t<float, 2, kEpBlindRotate, 2, L>(P, T, a, st);
         if (groups == 4) return launch_ep_t<float, 2, kEpBlindRotate, 4, L>(P, T, a, st);

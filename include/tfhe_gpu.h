@@ -102,8 +102,9 @@ size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
 
 /* Launch shape of the blind-rotation kernel of `form`.  split-FP32:
  *   0 = automatic: whole waves of 6 ciphertexts per SM on shape 10; a
- *       remainder of at most 2 per SM on the pair kernel, of at most 4 per
- *       SM as one shape-9 wave, else one more shape-10 wave;
+ *       remainder of at most 1 per SM on shape 14, of 2 per SM on the pair
+ *       kernel, of at most 4 per SM as one shape-9 wave, else one more
+ *       shape-10 wave;
  *   1, 2, 4 = ciphertexts (64 threads each) per CTA, key rows read from L2
  *       by every ciphertext;
  *   5 = 5 per CTA, key rows streamed once per CTA into a shared-memory ring
@@ -113,7 +114,10 @@ size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
  *       transforms run together (about 250 registers a thread);
  *   10 = 6 per CTA on the same ring, transforms two at a time;
  *   11, 12, 13 = pair kernel: two 64-thread halves per ciphertext (about
- *       half the latency), 1, 2, 3 ciphertexts per CTA, shared ring.
+ *       half the latency), 1, 2, 3 ciphertexts per CTA, shared ring;
+ *   14 = spread kernel: one ciphertext over 2l groups of 64 threads, one
+ *       forward and one inverse transform per group and step (lowest
+ *       latency), key rows from L2.
  * FP64: 3 (L2) or 4 (ring, in line).  Engine tuning knob, no counterpart in
  * the reference (its kernel is a single HLS work-item). */
 tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,

@@ -229,7 +229,7 @@ def test_errors_are_status_codes(pkg, keys, torch_cuda, P):
                                          ("split_fp32", 4), ("split_fp32", 5), ("split_fp32", 6),
                                          ("split_fp32", 7), ("split_fp32", 8), ("split_fp32", 9),
                                          ("split_fp32", 10), ("split_fp32", 11), ("split_fp32", 12),
-                                         ("split_fp32", 13),
+                                         ("split_fp32", 13), ("split_fp32", 14),
                                          ("fp64", 3), ("fp64", 4)])
 def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, groups):
     """Each blind-rotation launch shape (L2-direct and shared-ring kernels) on
@@ -260,13 +260,13 @@ def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, grou
     assert np.abs(d).max() <= PHASE_TOL
 
 
-@pytest.mark.parametrize("tail", [40, 400])
+@pytest.mark.parametrize("tail", [40, 200, 400])
 def test_auto_shape_full_wave_and_tail(pkg, oracle, keys, torch_cuda, P, inputs, tail):
     """The automatic split-FP32 shape on one full wave (6 per SM on the ring
-    kernel with transforms two at a time) plus a tail on the pair kernel (40)
-    or on the 4-per-SM batched ring kernel (400): every output decrypts to
-    the truth and ciphertexts from both launches match the oracle's
-    phases."""
+    kernel with transforms two at a time) plus a tail on the spread kernel
+    (40), the pair kernel (200) or the 4-per-SM batched ring kernel (400):
+    every output decrypts to the truth and ciphertexts from both launches
+    match the oracle's phases."""
     torch = torch_cuda
     a, b, ca, cb = inputs
     count = 6 * 152 + tail
@@ -368,14 +368,14 @@ def test_stress_set_noise_band(pkg, torch_cuda):
         e.close()
 
 
-@pytest.mark.parametrize("groups,count", [(0, 8), (6, 6), (9, 9), (10, 7), (13, 5), (5, 5)])
+@pytest.mark.parametrize("groups,count", [(11, 8), (6, 6), (9, 9), (10, 7), (13, 5), (5, 5)])
 def test_bounded_waits_report_timeout(pkg, oracle, keys, torch_cuda, P, inputs, groups, count):
     """The device-side failure path without a fault: a blind rotation whose
     key-row stream never starts (a flag the producer honours) makes every
     consumer's bounded wait run out; the kernel ends within a few seconds,
     the host gets TFHE_GPU_TIMEOUT, and the same context then bootstraps
-    correctly.  Shapes: automatic (pair kernel), ring in line, the two
-    batched rings, pair, ring with a producer warp."""
+    correctly.  Shapes: pair (1 and 3 per CTA), ring in line, the two
+    batched rings, ring with a producer warp."""
     import time
     torch = torch_cuda
     e = pkg.Engine(pkg.default_params())
@@ -400,22 +400,28 @@ def test_bounded_waits_report_timeout(pkg, oracle, keys, torch_cuda, P, inputs, 
         e.close()
 
 
-def test_l2_shape_has_no_waits(pkg, keys, torch_cuda):
+def test_l2_shapes_have_no_waits(pkg, keys, torch_cuda):
+    """Shapes that read key rows straight from L2 (FP64 shape 3, and the
+    split-FP32 spread kernel that small batches take automatically) have no
+    key ring to stall: the self-test finds no timeout."""
     e = pkg.Engine(pkg.default_params())
     try:
-        e.upload_bootstrapping_key(keys["bk"], forms=("fp64",))
+        e.upload_bootstrapping_key(keys["bk"], forms=("fp64", "split_fp32"))
         e.set_groups_per_cta("fp64", 3)
         assert e.selftest_timeout("fp64", 3) == 0
+        assert e.get_groups_per_cta("split_fp32") == 0
+        assert e.selftest_timeout("split_fp32", 8) == 0
     finally:
         e.close()
 
 
-@pytest.mark.parametrize("count", [304, 305, 608, 609, 912, 913, 1216, 1217, 1520, 1521])
+@pytest.mark.parametrize("count", [152, 153, 304, 305, 608, 609, 912, 913, 1064, 1065, 1216, 1217, 1520, 1521])
 def test_auto_shape_boundaries(pkg, engine, oracle, keys, torch_cuda, P, count):
-    """Batch sizes on both sides of the automatic shape's boundaries: pair
-    kernel only up to 2 per SM; one 4-per-SM wave up to 4 per SM; 6-per-SM
-    waves; a wave plus a pair tail, plus a 4-per-SM tail, plus a partial
-    6-per-SM wave: every output decrypts to the truth."""
+    """Batch sizes on both sides of the automatic shape's boundaries: the
+    spread kernel up to 1 per SM, the pair kernel up to 2 per SM; one
+    4-per-SM wave up to 4 per SM; 6-per-SM waves; a wave plus a spread tail,
+    a pair tail, a 4-per-SM tail, or a partial 6-per-SM wave: every output
+    decrypts to the truth."""
     torch = torch_cuda
     rng = np.random.default_rng(97 + count)
     a = rng.integers(0, 2, count)
