@@ -165,15 +165,20 @@ tfhe_gpu_status run_gates_in(tfhe_gpu_ctx* ctx, const int32_t* gates, int32_t un
     const int n = ctx->P.n, nk = ctx->P.k * ctx->P.N;
     RET(run_bootstrap_woks(ctx, x, mu, u, split, form, st));
     CK(ctx, cudaEventRecord(ctx->ev_fork, st));
-    RET(run_bootstrap_woks(ctx, x + (size_t)split * (n + 1), mu, u + (size_t)split * (nk + 1), count - split,
-                           form, st));
     CK(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
     CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, u, out, split, ctx->side));
     CK(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
-    CK(ctx, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, u + (size_t)split * (nk + 1),
-                             out + (size_t)split * (n + 1), count - split, st));
-    CK(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
-    return TFHE_GPU_OK;
+    // from here on the caller's stream joins the side stream on every path
+    tfhe_gpu_status s = run_bootstrap_woks(ctx, x + (size_t)split * (n + 1), mu, u + (size_t)split * (nk + 1),
+                                           count - split, form, st);
+    if (s == TFHE_GPU_OK) {
+        const cudaError_t e = launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, u + (size_t)split * (nk + 1),
+                                               out + (size_t)split * (n + 1), count - split, st);
+        if (e != cudaSuccess) s = cuda_fail(ctx, e, "key switch");
+    }
+    const cudaError_t e = cudaStreamWaitEvent(st, ctx->ev_join, 0);
+    if (s == TFHE_GPU_OK && e != cudaSuccess) s = cuda_fail(ctx, e, "join");
+    return s;
 }
 
 tfhe_gpu_status run_gates(tfhe_gpu_ctx* ctx, const int32_t* gates, int32_t uniform_gate,
