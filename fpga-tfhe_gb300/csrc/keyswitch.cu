@@ -11,7 +11,7 @@
 // with rows padded to a multiple of 4 words (16-byte loads).  A CTA owns G
 // ciphertexts and a span of n_in / split input coefficients; each thread owns
 // four output coefficients (one 16-byte column) of all G of them, in
-// registers.  The CTA walks its (i, j) pairs once: for four levels j at a
+// registers.  The CTA walks its (i, j) pairs once: for two levels j at a
 // time it loads the base-1 non-zero rows of each level (independent 16-byte
 // loads, coalesced across the warp), then applies them to its G ciphertexts.
 // The digits are computed once per CTA in the prologue (8 digits of 2 bits
@@ -29,7 +29,7 @@ namespace tfhe_gb300 {
 namespace {
 
 constexpr int kKsGroup = 8;  // ciphertexts per CTA
-constexpr int kKsJBlock = 4; // digit levels loaded together
+constexpr int kKsJBlock = 2;  // digit levels loaded together (measured best: 63 registers, 6 CTAs per SM)
 
 __device__ __forceinline__ void sub4(uint4& a, const uint4& r) {
     a.x -= r.x;
