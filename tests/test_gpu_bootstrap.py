@@ -438,3 +438,27 @@ def test_auto_shape_boundaries(pkg, engine, oracle, keys, torch_cuda, P, count):
     names = sorted(pyoracle.GATES, key=lambda g: pyoracle.GATES[g])
     truth = np.array([pyoracle.GATE_FN[names[g]](x, y) for g, x, y in zip(gates, a, b)])
     assert (pkg.decrypt_bits(P, host(d_out), keys["lwe"]) == truth).all()
+
+
+@pytest.mark.parametrize("count", [1, 4096])
+def test_automatic_shape_is_deterministic(pkg, engine, keys, torch_cuda, P, count):
+    """The same batch twice gives bit-identical ciphertexts: a single gate on
+    the spread kernel (partial products summed in a fixed order, integer
+    atomics into the accumulator) and a 4096-gate layer whose first key
+    switch runs on the side stream during the remainder wave."""
+    torch = torch_cuda
+    rng = np.random.default_rng(201 + count)
+    a = rng.integers(0, 2, count)
+    b = rng.integers(0, 2, count)
+    pkg.set_seed([201 + count])
+    d_ca = dev(torch, pkg.encrypt_bits(P, a, keys["lwe"]))
+    d_cb = dev(torch, pkg.encrypt_bits(P, b, keys["lwe"]))
+    gates = dev(torch, rng.integers(0, 10, count).astype(np.int32))
+    outs = []
+    for _ in range(2):
+        d_out = torch.zeros((count, P.n + 1), dtype=torch.int32, device="cuda")
+        engine.bootsGates(gates, d_out, d_ca, d_cb, count, "split_fp32", stream=cur(torch))
+        torch.cuda.synchronize()
+        engine.synchronize()
+        outs.append(host(d_out))
+    assert (outs[0] == outs[1]).all()
