@@ -462,3 +462,33 @@ def test_automatic_shape_is_deterministic(pkg, engine, keys, torch_cuda, P, coun
         engine.synchronize()
         outs.append(host(d_out))
     assert (outs[0] == outs[1]).all()
+
+
+@pytest.mark.parametrize("count", [912 + 100, 912 + 400])
+def test_stress_set_split_batches(pkg, torch_cuda, count):
+    """The alternative set (l = 2) through the split automatic shape: a
+    6-per-SM wave plus a spread-kernel tail (1012), or plus a 4-per-SM tail
+    with the first key switch on the side stream (1312).  Every gate
+    decrypts to the truth except at the set's own failure rate (about 1e-5
+    per gate): at most one failure."""
+    torch = torch_cuda
+    P = pkg.stress_params()
+    lwe, tlwe, ks, bk = pkg.gate_keyset(P, [0])
+    e = pkg.Engine(P)
+    try:
+        e.upload_bootstrapping_key(bk, forms=("split_fp32",))
+        e.upload_keyswitch_key(ks)
+        rng = np.random.default_rng(211 + count)
+        a = rng.integers(0, 2, count)
+        b = rng.integers(0, 2, count)
+        pkg.set_seed([211 + count])
+        d_a = torch.from_numpy(pkg.encrypt_bits(P, a, lwe)).cuda()
+        d_b = torch.from_numpy(pkg.encrypt_bits(P, b, lwe)).cuda()
+        d_out = torch.empty_like(d_a)
+        e.bootsGate("AND", d_out, d_a, d_b, count, "split_fp32", stream=torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        e.synchronize()
+        fails = int((pkg.decrypt_bits(P, d_out.cpu().numpy(), lwe) != (a & b)).sum())
+        assert fails <= 1, fails
+    finally:
+        e.close()
