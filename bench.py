@@ -200,9 +200,19 @@ def cpu_baseline(seconds, batch_hint):
         el = time.perf_counter() - t0
         if el >= seconds:
             break
+    # one core: the per-gate latency of the CPU path (a few seconds)
+    one, t1 = 0, time.perf_counter()
+    while True:
+        o.boots_gate_batch(P, bk_fft, ks, gates[:1], ca[:1], cb[:1], 1)
+        one += 1
+        el1 = time.perf_counter() - t1
+        if el1 >= min(4.0, seconds / 2):
+            break
     return {"value": done / el, "unit": "bootstraps/s", "cores": threads, "kind": "port",
             "sample": "%d gate bootstraps (mixed NAND/AND/XOR/OR, default set) in %.1f s on %d threads"
-                      % (done, el, threads)}
+                      % (done, el, threads),
+            "single_core": {"bootstraps_per_s": one / el1, "gate_latency_ms": 1000.0 * el1 / one,
+                            "sample": "%d gates one after another on 1 thread in %.1f s" % (one, el1)}}
 
 
 def run_reference(args, world, rank):
