@@ -201,7 +201,7 @@ __device__ __forceinline__ FftTwiddles<R> hot_twiddles(const cpx<R>* hot) {
 //                 L1 prefetch of the rows ahead of the transform;
 //   RingKeys   -- from a shared-memory ring filled by a producer warp with
 //                 bulk copies (see k_blind_rotate_ring).
-// FB digit polynomials are transformed together (fft512_forward_multi), and
+// FB digit polynomials are transformed together (fft512_forward_tw_multi), and
 // IB parts of an output polynomial are transformed back together.
 // ----------------------------------------------------------------------
 template <typename R, int PARTS, int NB>

@@ -264,76 +264,6 @@ __device__ __forceinline__ void fft512_inverse(cpx<R> (&v)[8], const FftScratch<
     dft8<-1>(v);
 }
 
-// NB independent transforms at once (each with its own ping-pong pair of
-// buffers s[b]): the same three passes, but every pass works on NB point
-// sets before the group barrier, so each barrier phase carries NB times the
-// arithmetic and the registers hold NB independent dependency chains.
-template <int NB, typename R>
-__device__ __forceinline__ void fft512_forward_multi(cpx<R> (&v)[NB][8], const FftScratch<R> (&s)[NB],
-                                                     const FftTwiddles<R>& tw, int t, int bar_id) {
-#pragma unroll
-    for (int b = 0; b < NB; ++b) {
-        dft8<1>(v[b]);
-#pragma unroll
-        for (int q = 1; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.a[q * 64 + t]);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b0[slot<R>(t + 64 * q)] = v[b][q];
-    }
-    group_sync(bar_id);
-    const int hb = t >> 3, j = t & 7;
-#pragma unroll
-    for (int b = 0; b < NB; ++b) {
-#pragma unroll
-        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b0[slot<R>(64 * hb + j + 8 * r)];
-        dft8<1>(v[b]);
-#pragma unroll
-        for (int q = 1; q < 8; ++q) v[b][q] = cmul(v[b][q], tw.b[q * 8 + j]);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b1[slot<R>(64 * hb + j + 8 * q)] = v[b][q];
-    }
-    group_sync(bar_id);
-#pragma unroll
-    for (int b = 0; b < NB; ++b) {
-#pragma unroll
-        for (int r = 0; r < 8; ++r) v[b][r] = s[b].b1[slot<R>(8 * t + r)];
-        dft8<1>(v[b]);
-    }
-}
-
-template <int NB, typename R>
-__device__ __forceinline__ void fft512_inverse_multi(cpx<R> (&v)[NB][8], const FftScratch<R> (&s)[NB],
-                                                     const FftTwiddles<R>& tw, int t, int bar_id) {
-#pragma unroll
-    for (int b = 0; b < NB; ++b) {
-        dft8<-1>(v[b]);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b0[slot<R>(8 * t + q)] = v[b][q];
-    }
-    group_sync(bar_id);
-    const int hb = t >> 3, j = t & 7;
-#pragma unroll
-    for (int b = 0; b < NB; ++b) {
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            v[b][r] = s[b].b0[slot<R>(64 * hb + j + 8 * r)];
-            if (r) v[b][r] = cmulc(v[b][r], tw.b[r * 8 + j]);
-        }
-        dft8<-1>(v[b]);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) s[b].b1[slot<R>(64 * hb + j + 8 * q)] = v[b][q];
-    }
-    group_sync(bar_id);
-#pragma unroll
-    for (int b = 0; b < NB; ++b) {
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            v[b][r] = s[b].b1[slot<R>(t + 64 * r)];
-            if (r) v[b][r] = cmulc(v[b][r], tw.a[r * 64 + t]);
-        }
-        dft8<-1>(v[b]);
-    }
-}
-
 // Per-thread exchange slots of the FP32 swizzle, in closed form for each
 // access pattern (computed once per thread; an access is then an immediate
 // offset or one XOR):
