@@ -82,6 +82,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 }
 // Bulk copy global -> this CTA's shared memory; completion is counted in
 // bytes on `bar`.  dst, src 16-byte aligned; bytes a multiple of 16.
+// Start fetching `bytes` (a multiple of 16, 16-byte aligned) of global
+// memory into L2 without waiting for it.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes,
                                               uint64_t* bar) {
     asm volatile(

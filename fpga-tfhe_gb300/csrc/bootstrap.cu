@@ -828,24 +828,25 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
 // Blind rotation with one ciphertext over 2l groups (lowest latency).
 //
 // Group g = (jp, lev) = (g / l, g % l) decomposes input polynomial jp at
-// level lev, runs that one forward transform, multiplies it with its key
-// row (read from L2; the next step's row is prefetched into L1) and writes
-// the partial products of both outputs and both key parts to shared memory.
-// After a CTA barrier, group (j, pt) = (g / 2, g % 2) for g < 4 sums the 2l
-// partials of output j, part pt in a fixed order, transforms back, rounds,
-// and adds its part into the accumulator with integer shared-memory atomics
-// (exact mod 2^32 in any order, so the result does not depend on timing).
-// A step's critical path is one forward and one inverse transform instead
-// of the pair kernel's l forward and PARTS inverse ones.  Split-FP32 only.
+// level lev, runs that one forward transform and writes the transformed
+// digits D_g to shared memory.  After a CTA barrier, owner group (j, pt) =
+// (g / 2, g % 2) for g < 4 multiplies all 2l of them with part (j, pt) of
+// each key row, transforms back, rounds, and adds its part into the
+// accumulator with integer shared-memory atomics (exact mod 2^32 in any
+// order, so the result does not depend on timing).  The owners issue their
+// key loads (4 float4 per row, from L2) before the barrier, so the latency
+// overlaps the other groups' transforms; the next step's rows are
+// prefetched into L2.  A step's critical path is one forward transform, 2l
+// rows of products and one inverse transform, against the pair kernel's l
+// forward and PARTS inverse transforms.  Split-FP32 only.
 // ----------------------------------------------------------------------
 template <int L>
 struct SpreadPlan {
     static constexpr int kGroups = 2 * L;
     static constexpr size_t tables = kHotSize * sizeof(cpx<float>);
     static constexpr size_t acc_off = tables;
-    static constexpr size_t part_off = acc_off + 2 * kN * sizeof(int32_t);
-    static constexpr size_t part = 4 * kHalf * sizeof(cpx<float>);  // [j * 2 + pt][q][t]
-    static constexpr size_t scratch_off = part_off + kGroups * part;
+    static constexpr size_t d_off = acc_off + 2 * kN * sizeof(int32_t);
+    static constexpr size_t scratch_off = d_off + kGroups * kHalf * sizeof(cpx<float>);
     static constexpr size_t scratch = 2 * kScratchStride * sizeof(cpx<float>);
     static constexpr size_t total = scratch_off + kGroups * scratch;
 };
@@ -853,14 +854,17 @@ struct SpreadPlan {
 template <int L>
 __global__ void __launch_bounds__(128 * L, 1) k_blind_rotate_spread(KParams kp, Tables T, EpArgs a) {
     using Plan = SpreadPlan<L>;
+    constexpr int kRows = 2 * L;
     constexpr int kRowElems = 2 * 2 * kHalf;  // complex values per key row
     extern __shared__ __align__(128) char smem[];
     cpx<float>* tables = reinterpret_cast<cpx<float>*>(smem);
     int32_t* acc = reinterpret_cast<int32_t*>(smem + Plan::acc_off);
-    cpx<float>* part = reinterpret_cast<cpx<float>*>(smem + Plan::part_off);
+    cpx<float>* dsh = reinterpret_cast<cpx<float>*>(smem + Plan::d_off);  // [g][q][t]
     const int c = blockIdx.x;
     const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
     const int jp = g / L, lev = g - jp * L;
+    const bool owner = g < 4;
+    const int oj = g >> 1, opt = g & 1;
     const int n = kp.n;
     load_hot_tables<float>(tables, T);
     if (a.acc_in) {
@@ -884,22 +888,20 @@ __global__ void __launch_bounds__(128 * L, 1) k_blind_rotate_spread(KParams kp, 
     const uint32_t mask = (1u << kp.Bgbit) - 1;
     const int decal = 32 - (lev + 1) * kp.Bgbit;
     const cpx<float>* gsw = reinterpret_cast<const cpx<float>*>(a.gsw);
-    const size_t step_elems = (size_t)2 * L * kRowElems;
+    const size_t step_elems = (size_t)kRows * kRowElems;
     const int32_t* bara = a.bara ? a.bara + (size_t)c * n : nullptr;
     const int32_t* xs = a.x ? a.x + (size_t)c * (n + 1) : nullptr;
     int a_next = bara ? bara[0] : mod_switch_2n(xs[0]);
-    {  // this group's first key row into L1
-        const char* row = reinterpret_cast<const char*>(gsw + (size_t)g * kRowElems);
-        for (int ln = t; ln < kRowElems * (int)sizeof(cpx<float>) / 128; ln += 64)
-            asm volatile("prefetch.global.L1 [%0];" ::"l"(row + (size_t)ln * 128));
-    }
+    if (threadIdx.x < kRows) bulk_prefetch_l2(gsw + (size_t)threadIdx.x * kRowElems, kRowElems * sizeof(cpx<float>));
 #pragma unroll 1
     for (int i = 0; i < n; ++i) {
         const int ai = a_next;
         if (i + 1 < n) a_next = bara ? bara[i + 1] : mod_switch_2n(xs[i + 1]);
         if (ai == 0) continue;  // tfhe_blindRotate_FFT.cpp:114 (uniform over the CTA)
-        const cpx<float>* row = gsw + (size_t)i * step_elems + (size_t)g * kRowElems;
-        // forward: polynomial jp of (X^a - 1) acc at level lev
+        const cpx<float>* step_keys = gsw + (size_t)i * step_elems;
+        if (i + 1 < n && threadIdx.x < kRows)  // the next step's rows into L2
+            bulk_prefetch_l2(step_keys + step_elems + (size_t)threadIdx.x * kRowElems,
+                             kRowElems * sizeof(cpx<float>));
         cpx<float> v[8];
         {
             const int32_t* src = acc + jp * kN;
@@ -913,40 +915,36 @@ __global__ void __launch_bounds__(128 * L, 1) k_blind_rotate_spread(KParams kp, 
             }
         }
         fft512_forward_tw(v, sc, tw, ix, t, bar_id);
-        cpx<float> out[2][2][8];
 #pragma unroll
-        for (int j = 0; j < 2; ++j)
+        for (int q = 0; q < 8; ++q) dsh[(g * 8 + q) * 64 + t] = v[q];
+        float4 kk[kRows][4];
+        if (owner) {
 #pragma unroll
-            for (int pt = 0; pt < 2; ++pt)
+            for (int p = 0; p < kRows; ++p) {
+                const float4* g4 =
+                    reinterpret_cast<const float4*>(step_keys + (size_t)p * kRowElems + (oj * 2 + opt) * kHalf);
 #pragma unroll
-                for (int q = 0; q < 8; ++q) out[j][pt][q] = {0.f, 0.f};
-        mac_row<float, 2, false>(out, v, row, t);
-        if (i + 1 < n) {  // next step's row into L1 while the others finish
-            const char* nrow = reinterpret_cast<const char*>(row + step_elems);
-            for (int ln = t; ln < kRowElems * (int)sizeof(cpx<float>) / 128; ln += 64)
-                asm volatile("prefetch.global.L1 [%0];" ::"l"(nrow + (size_t)ln * 128));
+                for (int qq = 0; qq < 4; ++qq) kk[p][qq] = __ldg(g4 + qq * 64 + t);
+            }
         }
-        cpx<float>* mine = part + (size_t)g * 4 * kHalf;
+        __syncthreads();  // every D written, every read of acc done
+        if (owner) {
+            cpx<float> o[8];
 #pragma unroll
-        for (int j = 0; j < 2; ++j)
+            for (int q = 0; q < 8; ++q) o[q] = {0.f, 0.f};
 #pragma unroll
-            for (int pt = 0; pt < 2; ++pt)
+            for (int p = 0; p < kRows; ++p)
 #pragma unroll
-                for (int q = 0; q < 8; ++q) mine[((j * 2 + pt) * 8 + q) * 64 + t] = out[j][pt][q];
-        __syncthreads();  // every partial written, every read of acc done
-        if (g < 4) {
-            const int j = g >> 1, pt = g & 1;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) v[q] = part[((j * 2 + pt) * 8 + q) * 64 + t];
-#pragma unroll
-            for (int gg = 1; gg < 2 * L; ++gg)
-#pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    v[q] = cadd(v[q], part[(size_t)gg * 4 * kHalf + ((j * 2 + pt) * 8 + q) * 64 + t]);
-            fft512_inverse_tw(v, sc, tw, ix, t, bar_id);
+                for (int qq = 0; qq < 4; ++qq) {
+                    const cpx<float> d0 = dsh[(p * 8 + 2 * qq) * 64 + t];
+                    const cpx<float> d1 = dsh[(p * 8 + 2 * qq + 1) * 64 + t];
+                    o[2 * qq] = cmac(o[2 * qq], d0, cpx<float>{kk[p][qq].x, kk[p][qq].y});
+                    o[2 * qq + 1] = cmac(o[2 * qq + 1], d1, cpx<float>{kk[p][qq].z, kk[p][qq].w});
+                }
+            fft512_inverse_tw(o, sc, tw, ix, t, bar_id);
             uint32_t c0[8] = {}, c1[8] = {};  // the low part adds into them
-            round_part<float, 2>(v, pt, kp.split, c0, c1);
-            int32_t* dst = acc + j * kN;
+            round_part<float, 2>(o, opt, kp.split, c0, c1);
+            int32_t* dst = acc + oj * kN;
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 const int x0 = t + 64 * q;
@@ -1579,7 +1577,7 @@ cudaError_t launch_ring_pairs(const DevParams& P, const Tables& T, const EpArgs&
 // Measured per launch (default set): a wave of 6 per SM on
 // launch_ring_pairs 6.6 ms (138K gates/s), of 4 per SM on
 // launch_ring_batched 4.6 ms (132K/s), whatever the fill of the wave; the
-// spread kernel 2.1 ms at 1 per SM (4.2 ms for two waves); the pair kernel
+// spread kernel 1.9 ms at 1 per SM (3.8 ms for two waves); the pair kernel
 // 2.6 ms at 1 per SM, 3.3 ms at 2, 5.1 ms at 3.  So: whole waves of 6 per
 // SM; a remainder of at most 1 per SM on the spread kernel, of 2 per SM on
 // the pair kernel, of at most 4 per SM as one launch_ring_batched wave, else

@@ -115,8 +115,9 @@ size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
  *   10 = 6 per CTA on the same ring, transforms two at a time;
  *   11, 12, 13 = pair kernel: two 64-thread halves per ciphertext (about
  *       half the latency), 1, 2, 3 ciphertexts per CTA, shared ring;
- *   14 = spread kernel: one ciphertext over 2l groups of 64 threads, one
- *       forward and one inverse transform per group and step (lowest
+ *   14 = spread kernel: one ciphertext over 2l groups of 64 threads; per
+ *       step each group runs one forward transform, and four of them
+ *       multiply all rows for one output part and transform it back (lowest
  *       latency), key rows from L2.
  * FP64: 3 (L2) or 4 (ring, in line).  Engine tuning knob, no counterpart in
  * the reference (its kernel is a single HLS work-item). */

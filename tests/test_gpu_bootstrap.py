@@ -443,7 +443,7 @@ def test_auto_shape_boundaries(pkg, engine, oracle, keys, torch_cuda, P, count):
 @pytest.mark.parametrize("count", [1, 4096])
 def test_automatic_shape_is_deterministic(pkg, engine, keys, torch_cuda, P, count):
     """The same batch twice gives bit-identical ciphertexts: a single gate on
-    the spread kernel (partial products summed in a fixed order, integer
+    the spread kernel (products summed in a fixed order, integer
     atomics into the accumulator) and a 4096-gate layer whose first key
     switch runs on the side stream during the remainder wave."""
     torch = torch_cuda
