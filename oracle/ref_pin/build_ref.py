@@ -31,7 +31,8 @@ HLS_SOURCES = [os.path.join(SRC, "tfhe_blindRotate_FFT", f) for f in (
     "tGswFFTExternMulToTLwe.cpp", "pease_fft.cpp", "TorusPolynomial_fft.cpp", "tLweFromFFTConvert.cpp",
     "tfhe_MuxRotate_FFT.cpp", "tfhe_blindRotate_FFT.cpp", "tGswTorus32PolynomialDecompH.cpp",
     # linked only: the by-value tGswFFTExternMulToTLwe refers to them; both
-    # carry the defects the survey lists (buffer overflow, '=' for '+='), and
+    # carry known defects (IntPolynomial_ifft.cpp:7 writes past its output,
+    # tLweFFTAddMulRTo.cpp:20 assigns where it should accumulate), and
     # nothing here calls them
     "IntPolynomial_ifft.cpp", "tLweFFTAddMulRTo.cpp")] + [
     os.path.join(SRC, "tfhe_bootstrap_woKS_FFT", "tfhe_bootstrap_woKS_FFT.cpp"),
