@@ -492,3 +492,33 @@ def test_stress_set_split_batches(pkg, torch_cuda, count):
         assert fails <= 1, fails
     finally:
         e.close()
+
+
+def test_shapes_agree_bit_for_bit(pkg, keys, torch_cuda, P, inputs):
+    """Every split-FP32 shape that sums the 2l key rows in order (L2-direct
+    1/2/4, the rings 5-10, the spread kernel 14) runs the same transforms
+    and products in the same order, so their ciphertexts are identical bit
+    for bit.  The pair kernel adds the two halves' partial products and may
+    differ in the last rounding; it is held to the phase tolerance in the
+    other tests."""
+    torch = torch_cuda
+    a, b, ca, cb = inputs
+    count = 37
+    gates = dev(torch, (np.arange(count, dtype=np.int32) * 3) % 10)
+    e = pkg.Engine(pkg.default_params())
+    outs = {}
+    try:
+        e.upload_bootstrapping_key(keys["bk"], forms=("split_fp32",))
+        e.upload_keyswitch_key(keys["ks"])
+        for shape in (1, 2, 4, 5, 6, 7, 8, 9, 10, 14):
+            e.set_groups_per_cta("split_fp32", shape)
+            d_out = torch.zeros((count, P.n + 1), dtype=torch.int32, device="cuda")
+            e.bootsGates(gates, d_out, dev(torch, ca[:count]), dev(torch, cb[:count]), count, "split_fp32",
+                         stream=cur(torch))
+            torch.cuda.synchronize()
+            e.synchronize()
+            outs[shape] = host(d_out)
+    finally:
+        e.close()
+    for shape, out in outs.items():
+        assert (out == outs[6]).all(), shape
