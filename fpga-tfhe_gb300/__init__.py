@@ -484,6 +484,11 @@ class Engine:
         return self.lib.tfhe_gpu_device_bytes(self.ctx)
 
     def set_groups_per_cta(self, form, groups):
+        """Launch shape of the blind rotation (tfhe_gpu_set_groups_per_cta).
+        split_fp32: 0 automatic; 1, 2, 4 L2-direct; 5-8 shared key ring, one
+        transform at a time; 9 ring, 4 per CTA, a step's transforms
+        together; 10 ring, 6 per CTA, two at a time; 11-13 pair kernel;
+        14 spread kernel (lowest latency).  fp64: 3 or 4."""
         self._check(self.lib.tfhe_gpu_set_groups_per_cta(self.ctx, self._form(form), int(groups)),
                     "set_groups_per_cta")
 
@@ -533,7 +538,8 @@ class Engine:
 
     def autotune(self, form, count):
         """Time the launch shapes on `count` ciphertexts; keeps and returns
-        (shape, ms) of the fastest."""
+        (shape, ms) of the fastest (the automatic shape unless another is
+        more than 2 % faster)."""
         shape = ctypes.c_int32()
         ms = ctypes.c_float()
         self._check(self.lib.tfhe_gpu_autotune(self.ctx, self._form(form), int(count), ctypes.byref(shape),
