@@ -1,0 +1,48 @@
+"""bench.py's launch accounting (kernel names, blind-rotation launches per
+step for the roofline traffic, eager launch count) restates the engine's
+automatic split-FP32 shape (launch_auto_fp32 in csrc/bootstrap.cu, rule in
+include/tfhe_gpu.h): whole waves of 6 per SM on shape 10; a remainder of at
+most 1 per SM on the spread kernel, 2 per SM on the pair kernel, at most 4
+per SM as one shape-9 wave, else one more shape-10 wave.  CPU only."""
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+bench = pytest.importorskip("bench")
+
+PAIRS = "k_blind_rotate_ring<float,2,6,3,4,inline,nb2>"
+BATCHED = "k_blind_rotate_ring<float,2,4,3,4,inline,nb3>"
+SPREAD = "k_blind_rotate_spread<3>"
+PAIR2 = "k_blind_rotate_pair<float,2,2,3,4>"
+
+
+@pytest.mark.parametrize("batch,want", [
+    (1, [SPREAD + " x 1"]),
+    (152, [SPREAD + " x 152"]),
+    (153, [PAIR2 + " x 153"]),
+    (304, [PAIR2 + " x 304"]),
+    (305, [BATCHED + " x 305"]),
+    (608, [BATCHED + " x 608"]),
+    (609, [PAIRS]),
+    (912, [PAIRS]),
+    (913, [PAIRS + " x 912", SPREAD + " x 1"]),
+    (1216, [PAIRS + " x 912", PAIR2 + " x 304"]),
+    (1520, [PAIRS + " x 912", BATCHED + " x 608"]),
+    (1521, [PAIRS]),
+    (4096, [PAIRS + " x 3648", BATCHED + " x 448"]),
+])
+def test_automatic_shape_launches(batch, want):
+    assert bench.blind_rotate_kernels("split_fp32", 0, batch) == want
+
+
+def test_explicit_shapes_and_other_set():
+    assert bench.blind_rotate_kernels("split_fp32", 9, 100) == [BATCHED]
+    assert bench.blind_rotate_kernels("split_fp32", 10, 100) == [PAIRS]
+    assert bench.blind_rotate_kernels("split_fp32", 14, 5) == [SPREAD]
+    assert bench.blind_rotate_kernels("split_fp32", 12, 5) == [PAIR2]
+    assert bench.blind_rotate_kernels("split_fp32", 10, 100, l=2) == ["k_blind_rotate_ring<float,2,6,2,4,inline,nb2>"]
+    assert bench.blind_rotate_kernels("fp64", 3, 100) == ["k_external_product<double,1,BlindRotate,3,3>"]
