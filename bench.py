@@ -743,7 +743,7 @@ def main():
         one = statistics.median(one_ms[1:])
         # a single gate on the automatic shape (pair kernel), whatever shape
         # the autotuner kept for the full batch
-        tuned = eng.get_groups_per_cta("split_fp32")
+        saved_shape = eng.get_groups_per_cta("split_fp32")
         eng.set_groups_per_cta("split_fp32", 0)
         one32 = []
         for s in range(4):
@@ -754,7 +754,7 @@ def main():
             e1.record(stream)
             torch.cuda.synchronize()
             one32.append(e0.elapsed_time(e1))
-        eng.set_groups_per_cta("split_fp32", tuned)
+        eng.set_groups_per_cta("split_fp32", saved_shape)
         extras["split_fp32_single_gate_ms"] = statistics.median(one32[1:])
         extras["fp64_single_gate_ms"] = one
         extras["fp64_single_gate_bootstraps_per_s"] = 1000.0 / one

@@ -20,9 +20,13 @@
 //
 // Host code cannot use `g_noalloc_scratch` as an address (in host code the
 // name is a stand-in, not device memory).  The device address comes from
-// cudaGetSymbolAddress, looked up once per device, with that device current,
-// on the first call of this entry point on that device; make that first call
-// before capturing any stream into a graph.
+// cudaGetSymbolAddress, looked up with the device current on the first call
+// of this entry point in each CUDA context of that device, and cached per
+// device together with that context's unique id: after cudaDeviceReset, or
+// in another context on the same device, the id differs and the address is
+// looked up again instead of reusing one that belongs to a destroyed
+// context.  Make the first call in a context before capturing any stream
+// into a graph (the lookup can load the library's device code).
 //
 // All calls on a device share the array, and it keeps whatever the last call
 // left in it.  No word of it needs to start at zero: each call writes every
@@ -31,6 +35,7 @@
 // extracted sample).  Two calls whose work overlaps on the GPU -- on two
 // streams, or from two contexts on the same device -- race on the array:
 // serialise them.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -48,16 +53,51 @@ static __device__ __align__(256) int32_t g_noalloc_scratch[kNoAllocWords];
 constexpr int kMaxDevices = 64;
 std::mutex g_lock;
 int32_t* g_ptr[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device (looked up once).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the current CUDA context (ids are never reused within a
+// process, unlike context handles).  The driver functions come through the
+// runtime's entry-point query, so the library needs no link-time libcuda.
+cudaError_t current_context_id(unsigned long long* id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                                         cudaEnableDefault, &q1);
+        if (e != cudaSuccess) return e;
+        e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e != cudaSuccess) return e;
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return cudaErrorSymbolNotFound;
+        get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS || !c) return cudaErrorInvalidDevice;
+    if (get_id(c, id) != CUDA_SUCCESS) return cudaErrorInvalidDevice;
+    return cudaSuccess;
+}
+
+// Device address of g_noalloc_scratch in the current context of `device`
+// (looked up on the first call in each context, then cached).
 cudaError_t scratch_for_device(int device, int32_t** out) {
     if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> guard(g_lock);
-    if (!g_ptr[device]) {
+    unsigned long long id = 0;
+    cudaError_t e = current_context_id(&id);
+    if (e != cudaSuccess) return e;
+    if (!g_ptr[device] || g_ctx_id[device] != id) {
         void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
         g_ptr[device] = static_cast<int32_t*>(p);
+        g_ctx_id[device] = id;
     }
     *out = g_ptr[device];
     return cudaSuccess;

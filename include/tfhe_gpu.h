@@ -279,8 +279,10 @@ tfhe_gpu_status tfhe_gpu_bootsMUX_host(tfhe_gpu_ctx* ctx, int32_t* out, const in
  * cudaMalloc/cudaFree would synchronise the device, frameworks that own all
  * device memory).  No counterpart in the reference.  Limit: count x
  * (n + 1 + kN + 1) int32 words <= 847,872 (512 gates of the default set);
- * larger calls return TFHE_GPU_BAD_PARAM.  The first call on a device looks
- * up the array's address (make it before any stream capture).  Calls that
+ * larger calls return TFHE_GPU_BAD_PARAM.  The first call in each CUDA
+ * context of a device looks up the array's address (make it before any
+ * stream capture); a later context, e.g. after cudaDeviceReset, gets its own
+ * lookup.  Calls that
  * overlap on the GPU share the array and race: serialise them. */
 tfhe_gpu_status tfhe_gpu_bootsGates_noalloc(tfhe_gpu_ctx* ctx, const int32_t* gates,
                                             int32_t* out, const int32_t* ca,

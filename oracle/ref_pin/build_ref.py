@@ -1,5 +1,5 @@
 """Build recipe of oracle/_ref/: the reference's own CPU-path sources,
-compiled where they lie under /root/reference (never copied), against
+compiled where they lie in the reference checkout (never copied), against
 self-written stand-ins for the headers they need and do not ship:
 
   * libref_hls.so  -- kernel/src/tfhe_blindRotate_FFT/{tGswFFTExternMulToTLwe,
@@ -24,7 +24,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-REF = "/root/reference"
+# the reference checkout: TFHE_REFERENCE_DIR, else the usual mount point of
+# the read-only reference on the build machine
+REF = os.environ.get("TFHE_REFERENCE_DIR", "/root/reference")
 SRC = os.path.join(REF, "kernel", "src")
 
 HLS_SOURCES = [os.path.join(SRC, "tfhe_blindRotate_FFT", f) for f in (

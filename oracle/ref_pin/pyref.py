@@ -2,11 +2,15 @@
 build_ref.py).  Test infrastructure only.
 
 The reference's MuxRotate and blind-rotation files open text log files in
-the working directory when the library loads (tfhe_MuxRotate_FFT.cpp:5-7)
-and write every polynomial to them; the loader switches to a private
-temporary directory while loading so that those files land there.
+the working directory: MuxRotate when the library loads
+(tfhe_MuxRotate_FFT.cpp:5-7), the blind rotation on every call
+(tfhe_blindRotate_FFT.cpp:85).  The loader switches to a private temporary
+directory while loading and around every call into the hot-path library, so
+that those files land there and never in the caller's directory.
 """
+import contextlib
 import ctypes
+import functools
 import os
 import tempfile
 
@@ -23,6 +27,15 @@ _REF = None
 
 def _p(a, t):
     return a.ctypes.data_as(t)
+
+
+def _in_logdir(method):
+    """Run a method that calls into libref_hls.so from the log directory."""
+    @functools.wraps(method)
+    def wrapped(self, *args, **kwargs):
+        with self.logs():
+            return method(self, *args, **kwargs)
+    return wrapped
 
 
 class Reference:
@@ -72,6 +85,16 @@ class Reference:
         H.refh_params(_p(pv, I32P))
         self.n, self.N, self.k, self.l, self.Bgbit, self.ks_t, self.ks_basebit = (int(x) for x in pv)
 
+    @contextlib.contextmanager
+    def logs(self):
+        """Working directory = the private log directory for the duration."""
+        cwd = os.getcwd()
+        os.chdir(self.logdir)
+        try:
+            yield
+        finally:
+            os.chdir(cwd)
+
     # numeric / LWE (numeric-functions.cpp, lwe-functions.cpp)
     def set_seed(self, values):
         v = np.ascontiguousarray(values, np.uint32)
@@ -110,38 +133,45 @@ class Reference:
         return out
 
     # hot-path kernels (tfhe_blindRotate_FFT/*.cpp)
+    @_in_logdir
     def decompose(self, poly):
         out = np.zeros(self.l * self.N, np.int32)
         self.hls.refh_decompose(_p(np.ascontiguousarray(poly, np.int32), I32P), _p(out, I32P))
         return out.reshape(self.l, self.N)
 
+    @_in_logdir
     def decomp_h(self, poly):
         out = np.zeros(self.l * self.N, np.int32)
         self.hls.refh_decomp_h(_p(np.ascontiguousarray(poly, np.int32), I32P), _p(out, I32P))
         return out.reshape(self.l, self.N)
 
+    @_in_logdir
     def int_ifft(self, poly):
         out = np.zeros(self.N, np.float64)
         self.hls.refh_int_ifft(_p(np.ascontiguousarray(poly, np.int32), I32P), _p(out, F64P))
         return out[0::2] + 1j * out[1::2]
 
+    @_in_logdir
     def torus_fft(self, values):
         v = np.ascontiguousarray(np.stack([np.real(values), np.imag(values)], -1).reshape(-1), np.float64)
         out = np.zeros(self.N, np.int32)
         self.hls.refh_torus_fft(_p(v, F64P), _p(out, I32P))
         return out
 
+    @_in_logdir
     def extern_mul(self, accum, gsw_fft):
         acc = np.array(accum, np.int32, copy=True).reshape(-1)
         self.hls.refh_extern_mul(_p(acc, I32P), _p(np.ascontiguousarray(gsw_fft, np.float64), F64P))
         return acc
 
+    @_in_logdir
     def mux_rotate(self, accum, bki_fft, barai):
         out = np.zeros((self.k + 1) * self.N, np.int32)
         self.hls.refh_mux_rotate(_p(out, I32P), _p(np.ascontiguousarray(accum, np.int32), I32P),
                                  _p(np.ascontiguousarray(bki_fft, np.float64), F64P), int(barai))
         return out
 
+    @_in_logdir
     def blind_rotate(self, accum, bk_fft, bara):
         acc = np.array(accum, np.int32, copy=True).reshape(-1)
         bara = np.ascontiguousarray(bara, np.int32)
@@ -149,12 +179,14 @@ class Reference:
                                    _p(bara, I32P), len(bara))
         return acc
 
+    @_in_logdir
     def blind_rotate_shipped(self, accum, bk0_fft, bara):
         acc = np.array(accum, np.int32, copy=True).reshape(-1)
         self.hls.refh_blind_rotate_shipped(_p(acc, I32P), _p(np.ascontiguousarray(bk0_fft, np.float64), F64P),
                                            _p(np.ascontiguousarray(bara, np.int32), I32P))
         return acc
 
+    @_in_logdir
     def bootstrap_front(self, x, mu):
         tv = np.zeros(self.N, np.int32)
         bara = np.zeros(self.n, np.int32)
