@@ -110,6 +110,16 @@ def job_throughput(units_per_rank, world, max_ms):
     return world * units_per_rank / (max_ms / 1000.0)
 
 
+def layer_config(batch):
+    """The workload's `config`, identical in both arms (the reference arm
+    times a bounded sample of this workload and says so in its
+    cpu_baseline.sample)."""
+    return {"workload": "batched circuit layer: %d independent gate bootstraps, mixed NAND/AND/XOR/OR "
+                        "(seed 4), default 110-bit set (n=630, N=1024, k=1, l=3, Bgbit=7, t=8, basebit=2), "
+                        "one cloud key (seed 0)" % batch,
+            "batch": batch, "l2": "flushed (256 MB write) between timed steps", "parallelism": "replicas"}
+
+
 def make_inputs(pkg, P, lwe_key, batch, seed=4):
     rng = np.random.default_rng(seed)
     a = rng.integers(0, 2, batch)
@@ -247,12 +257,12 @@ def run_reference(args, world, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "batched circuit layer of mixed NAND/AND/XOR/OR gate bootstraps, "
-                               "default 110-bit set (n=630, N=1024, k=1, l=3, Bgbit=7, t=8, basebit=2); "
-                               "each step a bounded sample of %d gates of the 4096-gate layer" % n,
-                   "batch": n, "form": "fp64 (2N-point FFT restatement)"},
+        "config": layer_config(args.batch),
         "cpu_baseline": {"value": value, "unit": "bootstraps/s", "cores": threads, "kind": "port",
-                         "sample": "%d gates per step x %d steps" % (n, args.steps)},
+                         "sample": "each step a bounded sample of %d gates of the %d-gate layer (same gate "
+                                   "mix, keys and inputs), %d steps, FP64 2N-point transform restatement "
+                                   "of the reference path on %d host threads"
+                                   % (n, args.batch, args.steps, threads)},
         "e2e": {"value": value, "unit": "bootstraps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -380,82 +390,95 @@ def _measured_peak(key):
         return 6800.0 if key == "hbm_gbs" else None
 
 
-def workload_stress(args, world, rank, local):
-    """65536 NAND bootstraps on the alternative set n=500, l=2, Bgbit=10,
-    LWE 2^-15, TRLWE 2^-24: split-FP32 vs FP64, failure count and output
-    phase error.  (The comparison with the exact int64 bootstrap is a test:
-    tests/test_gpu_bootstrap.py::test_stress_set_against_exact.)"""
-    import __graft_entry__ as ge
-    pkg = ge.load_package()
+def run_stress(torch, pkg, local, split_bits=0, total=65536, batch=8192, forms=("split_fp32", "fp64")):
+    """`total` NAND bootstraps on the alternative set n=500, l=2, Bgbit=10,
+    LWE 2^-15, TRLWE 2^-24 (keys seed 0, inputs seed 4), in batches of
+    `batch`, per form: throughput, decryption failures and the output phase
+    error against the ideal +-1/8.  (Parity of this set against the oracle
+    and the exact int64 bootstrap is in the GPU tests.)"""
     P = pkg.stress_params()
-    P.split_bits = args.split_bits
-    torch, pkg, eng, keys, stream = _engine_setup(P, [0], local)
-    lwe, tlwe, ks, bk = keys
-    total = 65536
-    batch = 8192
-    rng = np.random.default_rng(4)
-    a = rng.integers(0, 2, total)
-    b = rng.integers(0, 2, total)
-    pkg.set_seed([4])
-    ca = pkg.encrypt_bits(P, a, lwe)
-    cb = pkg.encrypt_bits(P, b, lwe)
-    truth = 1 - (a & b)
-    sp = stream.cuda_stream
-    d_ca = torch.from_numpy(ca).cuda()
-    d_cb = torch.from_numpy(cb).cuda()
-    d_out = torch.empty_like(d_ca)
-    mu = 2 ** 29
-    res = {}
-    for form in ("split_fp32", "fp64"):
-        def run_all():
-            for s0 in range(0, total, batch):
-                eng.bootsGate("NAND", d_out[s0:s0 + batch], d_ca[s0:s0 + batch], d_cb[s0:s0 + batch],
-                              batch, form, stream=sp)
-        ms = _time_steps(torch, stream, run_all, 1, 1)
-        out = d_out.cpu().numpy()
-        bits = pkg.decrypt_bits(P, out, lwe)
-        ph = pkg.phases(out, lwe).astype(np.int64)
-        err = np.abs(np.abs(ph) - mu) / 2.0 ** 32
-        signed = ((ph - np.where(truth == 1, mu, -mu) + 2 ** 31) % 2 ** 32 - 2 ** 31) / 2.0 ** 32
-        res[form] = {"bootstraps_per_s": total / (ms[0] / 1000.0), "failures": int((bits != truth).sum()),
-                     "failed_gates": [int(i) for i in np.nonzero(bits != truth)[0][:16]],
-                     "gates": total, "phase_err_max_turn": float(err.max()),
-                     "phase_err_sigma_turn": float(signed.std()),
-                     "phase_err_mean_turn": float(err.mean()), "phase_err_std_turn": float(err.std())}
+    P.split_bits = split_bits
+    lwe, tlwe, ks, bk = pkg.gate_keyset(P, [0])
+    eng = pkg.Engine(P, device=local)
+    try:
+        eng.upload_bootstrapping_key(bk, forms=forms)
+        eng.upload_keyswitch_key(ks)
+        stream = torch.cuda.current_stream()
+        sp = stream.cuda_stream
+        rng = np.random.default_rng(4)
+        a = rng.integers(0, 2, total)
+        b = rng.integers(0, 2, total)
+        pkg.set_seed([4])
+        ca = pkg.encrypt_bits(P, a, lwe)
+        cb = pkg.encrypt_bits(P, b, lwe)
+        truth = 1 - (a & b)
+        d_ca = torch.from_numpy(ca).cuda()
+        d_cb = torch.from_numpy(cb).cuda()
+        d_out = torch.empty_like(d_ca)
+        mu = 2 ** 29
+        res = {"gates": total, "split_bits": eng.params.split_bits}
+        for form in forms:
+            def run_all():
+                for s0 in range(0, total, batch):
+                    eng.bootsGate("NAND", d_out[s0:s0 + batch], d_ca[s0:s0 + batch], d_cb[s0:s0 + batch],
+                                  batch, form, stream=sp)
+            ms = _time_steps(torch, stream, run_all, 1, 1)
+            out = d_out.cpu().numpy()
+            bits = pkg.decrypt_bits(P, out, lwe)
+            ph = pkg.phases(out, lwe).astype(np.int64)
+            err = np.abs(np.abs(ph) - mu) / 2.0 ** 32
+            signed = ((ph - np.where(truth == 1, mu, -mu) + 2 ** 31) % 2 ** 32 - 2 ** 31) / 2.0 ** 32
+            res[form] = {"bootstraps_per_s": total / (ms[0] / 1000.0), "failures": int((bits != truth).sum()),
+                         "failed_gates": [int(i) for i in np.nonzero(bits != truth)[0][:16]],
+                         "phase_err_max_turn": float(err.max()),
+                         "phase_err_sigma_turn": float(signed.std()),
+                         "phase_err_mean_turn": float(err.mean())}
+    finally:
+        eng.close()
+    return res
+
+
+def workload_stress(args, world, rank, local):
+    """Precision stress: 65,536 NAND on the n=500/l=2/Bgbit=10 set, split-FP32
+    vs FP64 (one JSON line)."""
+    import __graft_entry__ as ge
+    import torch
+    torch.cuda.set_device(local)
+    ge.build()
+    pkg = ge.load_package()
+    torch.cuda.set_stream(torch.cuda.Stream())
+    res = run_stress(torch, pkg, local, args.split_bits)
     f = res["split_fp32"]
+    total = res["gates"]
     line = {"metric": "gate bootstraps/sec", "value": f["bootstraps_per_s"], "unit": "bootstraps/s",
             "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": total / f["bootstraps_per_s"] * 1000,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": "precision stress: 65536 NAND bootstraps, n=500, N=1024, k=1, l=2, "
                                    "Bgbit=10, ks t=8 basebit=2, LWE 2^-15, TRLWE 2^-24 (keys seed 0, "
-                                   "inputs seed 4)", "batch": batch, "split_bits": eng.params.split_bits},
-            "forms": res}
+                                   "inputs seed 4)", "batch": 8192, "split_bits": res["split_bits"]},
+            "forms": {k: v for k, v in res.items() if k in ("split_fp32", "fp64")}}
     print(json.dumps(line), flush=True)
 
 
-def workload_failures(args, world, rank, local):
-    """10^6 gate bootstraps (default set, split-FP32) as 245 chained layers of
-    4096 random gates with random wiring: each layer's inputs are outputs of
-    the previous layer; every output decrypted and compared with plaintext
-    evaluation of the same circuit."""
-    import __graft_entry__ as ge
-    pkg = ge.load_package()
-    P = pkg.default_params()
-    P.split_bits = args.split_bits
-    torch, pkg, eng, keys, stream = _engine_setup(P, [0], local, forms=("split_fp32",))
-    lwe = keys[0]
-    width, layers = 4096, 245
+GATE_FNS = [lambda x, y: 1 - (x & y), lambda x, y: x & y, lambda x, y: x | y, lambda x, y: x ^ y,
+            lambda x, y: 1 - (x ^ y), lambda x, y: 1 - (x | y), lambda x, y: (1 - x) & y,
+            lambda x, y: x & (1 - y), lambda x, y: (1 - x) | y, lambda x, y: x | (1 - y)]
+
+
+def run_failures(torch, pkg, eng, P, lwe, width=4096, layers=245, form="split_fp32"):
+    """width x layers gate bootstraps as chained layers of random gates (all
+    10 gate types, random wiring, seed 7): each layer's inputs are outputs
+    of the previous layer; every output decrypted and compared with the
+    plaintext evaluation of the same circuit."""
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
     err_sum = err_sq = 0.0
     rng = np.random.default_rng(7)
     bits = rng.integers(0, 2, width)
     pkg.set_seed([7])
     cur = torch.from_numpy(pkg.encrypt_bits(P, bits, lwe)).cuda()
-    sp = stream.cuda_stream
     out = torch.empty_like(cur)
-    fns = [lambda x, y: 1 - (x & y), lambda x, y: x & y, lambda x, y: x | y, lambda x, y: x ^ y,
-           lambda x, y: 1 - (x ^ y), lambda x, y: 1 - (x | y), lambda x, y: (1 - x) & y,
-           lambda x, y: x & (1 - y), lambda x, y: (1 - x) | y, lambda x, y: x | (1 - y)]
     failures = 0
     worst = 0.0
     t0 = time.perf_counter()
@@ -466,13 +489,14 @@ def workload_failures(args, world, rank, local):
         g = rng.integers(0, 10, width).astype(np.int32)
         ca = cur[torch.from_numpy(ia).cuda()].contiguous()
         cb = cur[torch.from_numpy(ib).cuda()].contiguous()
+        d_g = torch.from_numpy(g).cuda()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        eng.bootsGates(torch.from_numpy(g).cuda(), out, ca, cb, width, "split_fp32", stream=sp)
+        eng.bootsGates(d_g, out, ca, cb, width, form, stream=sp)
         e1.record(stream)
         torch.cuda.synchronize()
         gpu_ms += e0.elapsed_time(e1)
-        nb = np.array([fns[gi](bits[x], bits[y]) for gi, x, y in zip(g, ia, ib)])
+        nb = np.array([GATE_FNS[gi](bits[x], bits[y]) for gi, x, y in zip(g, ia, ib)])
         host = out.cpu().numpy()
         got = pkg.decrypt_bits(P, host, lwe)
         failures += int((got != nb).sum())
@@ -484,45 +508,52 @@ def workload_failures(args, world, rank, local):
         bits = nb  # continue from the plaintext truth; the ciphertexts carry on
         cur, out = out, cur
     total = width * layers
-    line = {"metric": "decryption failures", "value": failures, "unit": "failures",
-            "gates": total, "n_gpus": 1, "steps": layers, "warmup": 0,
-            "ms_per_step": gpu_ms / layers, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "%d gate bootstraps: %d chained layers of %d random gates (all 10 "
-                                   "gate types, random wiring, seed 7), default set, split-FP32"
-                                   % (total, layers, width)},
-            "bootstraps_per_s": total / (gpu_ms / 1000.0),
+    return {"gates": total, "failures": failures, "bootstraps_per_s": total / (gpu_ms / 1000.0),
             "worst_phase_error_turn": worst,
-            "phase_error_sigma_turn": (err_sq / (width * layers) - (err_sum / (width * layers)) ** 2) ** 0.5,
-            "split_bits": eng.params.split_bits, "wall_s": time.perf_counter() - t0}
-    print(json.dumps(line), flush=True)
+            "phase_error_sigma_turn": (err_sq / total - (err_sum / total) ** 2) ** 0.5,
+            "form": form, "split_bits": eng.params.split_bits, "gpu_ms_per_layer": gpu_ms / layers,
+            "wall_s": time.perf_counter() - t0,
+            "workload": "%d chained layers of %d random gates (all 10 gate types, random wiring, seed 7), "
+                        "default set, %s" % (layers, width, form)}
 
 
-def workload_serve(args, world, rank, local):
-    """Serving: `clients` simulated clients, Poisson arrivals (rate per
-    client, seed 5), each request a random circuit -- 32-bit ripple-carry
-    adder (157 gates, depth 64), 16-bit comparator (cloud.c's compare_bit
-    chain, 16 XNOR + 16 MUX), 8-bit multiplexer (8 MUX) -- with random
-    operands, submitted to the continuous-batching server under one cloud
-    key.  Per-gate latency = gate ready -> bootstrapped; request latency =
-    arrival -> outputs back on the host.  Every output is decrypted and
-    checked."""
-    import importlib
+def workload_failures(args, world, rank, local):
+    """10^6 gate bootstraps (default set, split-FP32) as 245 chained layers of
+    4096 random gates, decryption checked (one JSON line)."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
     P = pkg.default_params()
-    torch, pkg, eng, keys, stream = _engine_setup(P, [0], local)
+    P.split_bits = args.split_bits
+    torch, pkg, eng, keys, stream = _engine_setup(P, [0], local, forms=("split_fp32",))
+    r = run_failures(torch, pkg, eng, P, keys[0])
+    line = {"metric": "decryption failures", "value": r["failures"], "unit": "failures",
+            "gates": r["gates"], "n_gpus": 1, "steps": 245, "warmup": 0,
+            "ms_per_step": r["gpu_ms_per_layer"], "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "%d gate bootstraps: " % r["gates"] + r["workload"]},
+            "bootstraps_per_s": r["bootstraps_per_s"],
+            "worst_phase_error_turn": r["worst_phase_error_turn"],
+            "phase_error_sigma_turn": r["phase_error_sigma_turn"],
+            "split_bits": r["split_bits"], "wall_s": r["wall_s"]}
+    print(json.dumps(line), flush=True)
+    eng.close()
+
+
+def serving_requests(pkg, P, lwe, clients, requests, rate, seed=5):
+    """Poisson request streams: `clients` clients, `rate` requests/s each;
+    each request a random circuit (32-bit ripple-carry adder, 16-bit
+    comparator, 8-bit multiplexer) with random operands."""
+    import importlib
     circuits = importlib.import_module("tfhe_gb300.circuits")
-    lwe = keys[0]
-    rng = np.random.default_rng(5)
+    rng = np.random.default_rng(seed)
     kinds = [("adder", circuits.ripple_carry_adder(32)), ("cmp", circuits.comparator(16)),
              ("mux", circuits.multiplexer(8))]
     reqs = []
-    pkg.set_seed([5])
-    for cl in range(args.clients):
+    pkg.set_seed([seed])
+    for cl in range(clients):
         t = 0.0
-        for _ in range(args.requests):
-            t += rng.exponential(1.0 / args.rate)
+        for _ in range(requests):
+            t += rng.exponential(1.0 / rate)
             k = int(rng.integers(0, 3))
             name, (gates, ni, outs) = kinds[k]
             bits = rng.integers(0, 2, ni).astype(np.int32)
@@ -531,43 +562,66 @@ def workload_serve(args, world, rank, local):
                          "want": circuits.evaluate(gates, bits, outs)})
     reqs.sort(key=lambda r: r["t"])
     total_boots = sum(circuits.bootstraps(r["gates"]) for r in reqs)
+    return reqs, total_boots
+
+
+def run_serving(pkg, eng, P, lwe, reqs, total_boots, form, pool_slots=131072, max_batch=4096):
+    """Replay the request streams against the continuous-batching server:
+    requests are submitted at their arrival times, the server steps while
+    work is pending, every output is decrypted and checked.  Per-gate
+    latency = gate ready -> bootstrapped; request latency = arrival ->
+    outputs back on the host."""
+    srv = pkg.Server(eng, pool_slots=pool_slots, max_batch=max_batch, form=form)
+    t0 = time.perf_counter()
+    nxt = 0
+    pending = {}
+    lat = {"adder": [], "cmp": [], "mux": []}
+    wrong = 0
+    while nxt < len(reqs) or pending:
+        now = time.perf_counter() - t0
+        while nxt < len(reqs) and reqs[nxt]["t"] <= now:
+            r = reqs[nxt]
+            pending[srv.submit(r["gates"], r["ni"], r["ct"], r["outs"])] = r
+            nxt += 1
+        ran = srv.step()
+        for rid in list(pending):
+            got = srv.poll(rid)
+            if got is not None:
+                r = pending.pop(rid)
+                lat[r["kind"]].append(time.perf_counter() - t0 - r["t"])  # from arrival
+                wrong += int((pkg.decrypt_bits(P, got[0], lwe) != r["want"]).any())
+        if ran == 0 and not pending and nxt < len(reqs):
+            time.sleep(max(0.0, reqs[nxt]["t"] - (time.perf_counter() - t0)))
+    makespan = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    gl = np.array(st["gate_latency_s"]) * 1000
+    allr = np.concatenate([np.array(v) for v in lat.values() if v]) * 1000
+    return {
+        "bootstraps_per_s": total_boots / makespan, "makespan_s": makespan,
+        "busy_s": st["busy_s"], "bootstraps_per_busy_s": total_boots / st["busy_s"],
+        "bootstraps": total_boots,
+        "gate_latency_ms": {"p50": float(np.percentile(gl, 50)), "p99": float(np.percentile(gl, 99))},
+        "request_latency_ms": {"p50": float(np.percentile(allr, 50)), "p99": float(np.percentile(allr, 99))},
+        "request_latency_ms_by_circuit": {k: {"p50": float(np.percentile(np.array(v) * 1000, 50)),
+                                              "p99": float(np.percentile(np.array(v) * 1000, 99)),
+                                              "n": len(v)} for k, v in lat.items() if v},
+        "requests": len(reqs), "wrong_requests": wrong}
+
+
+def workload_serve(args, world, rank, local):
+    """Serving: `clients` simulated clients with Poisson arrivals submitting
+    circuits to the continuous-batching server under one cloud key (one
+    JSON line)."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    P = pkg.default_params()
+    torch, pkg, eng, keys, stream = _engine_setup(P, [0], local)
+    lwe = keys[0]
+    reqs, total_boots = serving_requests(pkg, P, lwe, args.clients, args.requests, args.rate)
     result = {}
     for form in args.serve_forms.split(","):
-        srv = pkg.Server(eng, pool_slots=131072, max_batch=4096, form=form)
-        t0 = time.perf_counter()
-        nxt = 0
-        pending = {}
-        lat = {"adder": [], "cmp": [], "mux": []}
-        wrong = 0
-        while nxt < len(reqs) or pending:
-            now = time.perf_counter() - t0
-            while nxt < len(reqs) and reqs[nxt]["t"] <= now:
-                r = reqs[nxt]
-                pending[srv.submit(r["gates"], r["ni"], r["ct"], r["outs"])] = r
-                nxt += 1
-            ran = srv.step()
-            for rid in list(pending):
-                got = srv.poll(rid)
-                if got is not None:
-                    r = pending.pop(rid)
-                    lat[r["kind"]].append(time.perf_counter() - t0 - r["t"])  # from arrival
-                    wrong += int((pkg.decrypt_bits(P, got[0], lwe) != r["want"]).any())
-            if ran == 0 and not pending and nxt < len(reqs):
-                time.sleep(max(0.0, reqs[nxt]["t"] - (time.perf_counter() - t0)))
-        makespan = time.perf_counter() - t0
-        st = srv.stats()
-        srv.close()
-        gl = np.array(st["gate_latency_s"]) * 1000
-        allr = np.concatenate([np.array(v) for v in lat.values() if v]) * 1000
-        result[form] = {
-            "bootstraps_per_s": total_boots / makespan, "makespan_s": makespan,
-            "busy_s": st["busy_s"], "bootstraps_per_busy_s": total_boots / st["busy_s"],
-            "gate_latency_ms": {"p50": float(np.percentile(gl, 50)), "p99": float(np.percentile(gl, 99))},
-            "request_latency_ms": {"p50": float(np.percentile(allr, 50)), "p99": float(np.percentile(allr, 99))},
-            "request_latency_ms_by_circuit": {k: {"p50": float(np.percentile(np.array(v) * 1000, 50)),
-                                                  "p99": float(np.percentile(np.array(v) * 1000, 99)),
-                                                  "n": len(v)} for k, v in lat.items() if v},
-            "requests": len(reqs), "wrong_requests": wrong}
+        result[form] = run_serving(pkg, eng, P, lwe, reqs, total_boots, form)
     first = args.serve_forms.split(",")[0]
     f = result[first]
     line = {"metric": "gate bootstraps/sec (serving)", "value": f["bootstraps_per_s"],
@@ -585,6 +639,7 @@ def workload_serve(args, world, rank, local):
                            "request_p99": f["request_latency_ms"]["p99"]},
             "forms": result}
     print(json.dumps(line), flush=True)
+    eng.close()
 
 
 WORKLOADS = {"extprod": workload_extprod, "stress": workload_stress, "failures": workload_failures,
@@ -773,6 +828,16 @@ def main():
         extras["keygen_s"] = {"host": t_host, "gpu_arithmetic_with_upload": t_gpu,
                               "identical": all(bool((x == y).all()) for x, y in zip(host_keys, gpu_keys))}
         extras.update(side_paths(pkg, torch, eng, P, (lwe, tlwe, ks, bk), d_ca, d_cb, batch, stream, sp))
+        # the hard targets measured in the same run: decryption failures over
+        # 10^6 chained gates, the stress set's failure rate and noise in both
+        # forms, and serving latency under Poisson load
+        extras["failures"] = run_failures(torch, pkg, eng, P, lwe)
+        reqs, boots = serving_requests(pkg, P, lwe, args.clients, args.requests, args.rate)
+        extras["serving"] = run_serving(pkg, eng, P, lwe, reqs, boots, "split_fp32")
+        extras["serving"]["workload"] = ("%d clients x %d requests, Poisson %.1f req/s per client (seed 5), "
+                                         "32-bit adders, 16-bit comparators, 8-bit multiplexers, split-FP32"
+                                         % (args.clients, args.requests, args.rate))
+        extras["stress"] = run_stress(torch, pkg, local, args.split_bits)
         cpu = cpu_baseline(args.cpu_seconds, batch)
     else:
         cpu = None
@@ -786,13 +851,10 @@ def main():
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if args.form == "split_fp32" else "f64",
             "data": "synthetic",
-            "config": {"workload": "batched circuit layer: %d independent gate bootstraps, mixed "
-                                   "NAND/AND/XOR/OR (seed 4), default 110-bit set (n=630, N=1024, k=1, "
-                                   "l=3, Bgbit=7, t=8, basebit=2), one cloud key (seed 0)" % batch,
-                       "batch": batch, "form": args.form, "split_bits": eng.params.split_bits,
+            "config": layer_config(batch),
+            "engine": {"form": args.form, "split_bits": eng.params.split_bits,
                        "groups_per_cta": eng.get_groups_per_cta(args.form),
-                       "autotune": tuned, "cuda_graph": graph is not None,
-                       "l2": "flushed (256 MB write) between timed steps", "parallelism": "replicas"},
+                       "autotune": tuned, "cuda_graph": graph is not None},
             "latency_ms": {"p50": p50, "p99": p99,
                            "note": "per-gate latency = completion time of its batch"},
             "decrypt_ok": ok,

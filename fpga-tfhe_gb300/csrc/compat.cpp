@@ -8,6 +8,14 @@
 // samples into one contiguous host batch, run the engine's host-buffer entry
 // points and copy the results out, so a result may alias an input (cloud.c
 // does this at :21 and :12).
+//
+// With the environment variable TFHE_GB300_TRACE set (to anything), every
+// gate call prints one line to stderr: the call, its batch size, the device
+// it ran on and its host-side time.  It lets a user of an unmodified program
+// see that its gates ran on the GPU.
+#include <cuda_runtime.h>
+
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -89,9 +97,31 @@ tfhe_gpu_ctx* ready_ctx(const TFheGateBootstrappingCloudKeySet* bk, const char* 
     return I->ctx;
 }
 
+bool tracing() {
+    static const bool on = std::getenv("TFHE_GB300_TRACE") != nullptr;
+    return on;
+}
+
+const char* form_name(tfhe_gpu_form f) { return f == TFHE_GPU_FP64 ? "fp64" : "split_fp32"; }
+
+// one trace line per call (TFHE_GB300_TRACE)
+void trace(const char* fn, int32_t count, tfhe_gpu_form form,
+           std::chrono::steady_clock::time_point t0) {
+    const double ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    int dev = -1;
+    cudaDeviceProp prop{};
+    const bool ok = cudaGetDevice(&dev) == cudaSuccess &&
+                    cudaGetDeviceProperties(&prop, dev) == cudaSuccess;
+    std::fprintf(stderr, "tfhe_gb300 trace: %s: %d sample(s) on GPU %d (%s, sm_%d%d), %s form, %.3f ms\n",
+                 fn, count, dev, ok ? prop.name : "?", ok ? prop.major : 0, ok ? prop.minor : 0,
+                 form_name(form), ms);
+}
+
 void gate_batch(const char* fn, int32_t gate, LweSample* res, const LweSample* a, const LweSample* b,
                 int32_t count, const TFheGateBootstrappingCloudKeySet* bk) {
     if (count <= 0) return;
+    const auto t0 = std::chrono::steady_clock::now();
     if (!res || !a || !b) die(fn, "null sample");
     if (!bk || !bk->impl) die(fn, "null cloud keyset");
     std::lock_guard<std::mutex> lock(bk->impl->mu);
@@ -105,11 +135,13 @@ void gate_batch(const char* fn, int32_t gate, LweSample* res, const LweSample* a
                                                        I->in1.data(), count, I->form);
     if (s != TFHE_GPU_OK) die(fn, tfhe_gpu_last_error(ctx));
     unpack(res, I->out, count, n);
+    if (tracing()) trace(fn, count, I->form, t0);
 }
 
 void mux_batch(const char* fn, LweSample* res, const LweSample* a, const LweSample* b,
                const LweSample* c, int32_t count, const TFheGateBootstrappingCloudKeySet* bk) {
     if (count <= 0) return;
+    const auto t0 = std::chrono::steady_clock::now();
     if (!res || !a || !b || !c) die(fn, "null sample");
     if (!bk || !bk->impl) die(fn, "null cloud keyset");
     std::lock_guard<std::mutex> lock(bk->impl->mu);
@@ -124,6 +156,7 @@ void mux_batch(const char* fn, LweSample* res, const LweSample* a, const LweSamp
                                                      I->in2.data(), count, I->form);
     if (s != TFHE_GPU_OK) die(fn, tfhe_gpu_last_error(ctx));
     unpack(res, I->out, count, n);
+    if (tracing()) trace(fn, count, I->form, t0);
 }
 
 void free_impl(tfhe_compat_cloud* I) {

@@ -106,6 +106,11 @@ class Oracle:
             "orc_boots_mux": (None, [PP, F64P, I32P, I32P, I32P, I32P, I32P]),
             "orc_boots_gate_batch": (None, [PP, F64P, I32P, I32P, I32P, I32P, I32P,
                                             ctypes.c_int32, ctypes.c_int32]),
+            "orc_extern_mul_exact_batch": (None, [PP, I32P, I32P, ctypes.c_int32, ctypes.c_int32]),
+            "orc_bootstrap_woks_batch": (None, [PP, F64P, ctypes.c_int32, I32P, I32P, ctypes.c_int32,
+                                                ctypes.c_int32, I32P, ctypes.c_int32]),
+            "orc_boots_gate_exact_batch": (None, [PP, I32P, I32P, I32P, I32P, I32P, I32P,
+                                                  ctypes.c_int32, ctypes.c_int32]),
             "orc_max_threads": (ctypes.c_int32, []),
         }
         for name, (res, args) in sig.items():
@@ -310,6 +315,40 @@ class Oracle:
         out = np.zeros_like(ca)
         self.lib.orc_boots_gate_batch(ctypes.byref(P), _p(bk_fft, F64P), _p(ks, I32P), _p(gates, I32P),
                                       _p(ca, I32P), _p(cb, I32P), _p(out, I32P), len(gates), int(threads))
+        return out
+
+
+    def extern_mul_exact_batch(self, P, accum, gsw, threads=0):
+        """Exact int64 external products of count TRLWE samples (count x
+        (k+1)N) by count time-domain TGSW samples."""
+        acc = np.array(accum, np.int32, copy=True).reshape(-1, (P.k + 1) * P.N)
+        gsw = np.ascontiguousarray(gsw, np.int32).reshape(len(acc), -1)
+        self.lib.orc_extern_mul_exact_batch(ctypes.byref(P), _p(acc, I32P), _p(gsw, I32P), len(acc),
+                                            int(threads))
+        return acc
+
+    def bootstrap_woks_batch(self, P, bk_fft, mu, x, exact_bk=None, threads=0):
+        """Bootstraps without key switch of the samples x (count x (n+1)):
+        the FFT blind rotation, or the exact int64 one when exact_bk (the
+        time-domain key) is given."""
+        x = np.ascontiguousarray(x, np.int32).reshape(-1, P.n + 1)
+        out = np.zeros((len(x), P.k * P.N + 1), np.int32)
+        exact = exact_bk is not None
+        self.lib.orc_bootstrap_woks_batch(
+            ctypes.byref(P), _p(bk_fft, F64P) if bk_fft is not None else None, int(mu), _p(x, I32P),
+            _p(out, I32P), len(x), 1 if exact else 0,
+            _p(np.ascontiguousarray(exact_bk, np.int32), I32P) if exact else None, int(threads))
+        return out
+
+    def boots_gate_exact_batch(self, P, bk, ks, gates, ca, cb, threads=0):
+        """Gates through the exact int64 blind rotation (bk: time-domain key)."""
+        gates = np.ascontiguousarray(gates, np.int32)
+        ca = np.ascontiguousarray(ca, np.int32)
+        cb = np.ascontiguousarray(cb, np.int32)
+        out = np.zeros_like(ca)
+        self.lib.orc_boots_gate_exact_batch(ctypes.byref(P), _p(np.ascontiguousarray(bk, np.int32), I32P),
+                                            _p(ks, I32P), _p(gates, I32P), _p(ca, I32P), _p(cb, I32P),
+                                            _p(out, I32P), len(gates), int(threads))
         return out
 
 

@@ -490,22 +490,39 @@ void orc_extern_mul_fft(const orc_params* P, int32_t* accum,
         orc_torus_poly_fft(N, tmpa.data() + (size_t)j * N, accum + j * N);
 }
 
-/* The same product computed exactly: sum_p D_p * K_{p,j} negacyclic in
- * int64, reduced mod 2^32.  This is the "int64 negacyclic-product oracle". */
+/* The same product computed exactly: sum_p D_p * K_{p,j} negacyclic over
+ * the integers, reduced mod 2^32.  This is the "int64 negacyclic-product
+ * oracle".  The sums are carried in wrapping uint32 arithmetic: reduction
+ * mod 2^32 commutes with every + and x, so each word equals the int64 sum
+ * reduced at the end, bit for bit, and the loops vectorise on 32-bit lanes. */
 void orc_extern_mul_exact(const orc_params* P, int32_t* accum,
                           const int32_t* gsw) {
     const int32_t N = P->N, k = P->k, l = P->l, kpl = (k + 1) * l;
     std::vector<int32_t> deca((size_t)kpl * N);
     for (int32_t i = 0; i <= k; ++i)
         orc_decompose(P, accum + i * N, deca.data() + (size_t)i * l * N);
-    std::vector<int64_t> acc((size_t)(k + 1) * N, 0);
+    std::vector<uint32_t> acc((size_t)(k + 1) * N, 0);
+    std::vector<int32_t> nz;
     for (int32_t p = 0; p < kpl; ++p) {
         const int32_t* d = deca.data() + (size_t)p * N;
         for (int32_t j = 0; j <= k; ++j) {
-            const int32_t* g = gsw + (size_t)(p * (k + 1) + j) * N;
-            int64_t* o = acc.data() + (size_t)j * N;
+            const uint32_t* g = reinterpret_cast<const uint32_t*>(gsw) + (size_t)(p * (k + 1) + j) * N;
+            uint32_t* o = acc.data() + (size_t)j * N;
+            nz.clear();
+            for (int32_t t = 0; t < N && (int32_t)nz.size() * 8 <= N; ++t)
+                if (g[t]) nz.push_back(t);
+            if ((int32_t)nz.size() * 8 <= N) {
+                /* sparse key polynomial (e.g. a noiseless trivial TGSW):
+                 * the same sum, taken over its non-zero terms */
+                for (int32_t t : nz) {
+                    const uint32_t gt = g[t];
+                    for (int32_t i = 0; i < N - t; ++i) o[i + t] += (uint32_t)d[i] * gt;
+                    for (int32_t i = N - t; i < N; ++i) o[i + t - N] -= (uint32_t)d[i] * gt;
+                }
+                continue;
+            }
             for (int32_t s = 0; s < N; ++s) {
-                const int64_t ds = d[s];
+                const uint32_t ds = (uint32_t)d[s];
                 if (ds == 0) continue;
                 for (int32_t i = 0; i < s; ++i) o[i] -= ds * g[i - s + N];
                 for (int32_t i = s; i < N; ++i) o[i] += ds * g[i - s];
@@ -513,7 +530,7 @@ void orc_extern_mul_exact(const orc_params* P, int32_t* accum,
         }
     }
     for (int32_t i = 0; i < (k + 1) * N; ++i)
-        accum[i] = (int32_t)(uint32_t)(uint64_t)acc[i];
+        accum[i] = (int32_t)acc[i];
 }
 
 /* tfhe_MuxRotate_FFT.cpp:56-85: result = BK_i [(X^a - 1) acc] + acc.
@@ -744,6 +761,59 @@ void orc_boots_gate_batch(const orc_params* P, const double* bk_fft,
     for (int32_t g = 0; g < count; ++g)
         orc_boots_gate(P, bk_fft, ks, gates[g], ca + (size_t)g * w,
                        cb + (size_t)g * w, out + (size_t)g * w);
+    (void)threads;
+}
+
+/* `count` independent exact external products: accum (count x (k+1)N) by
+ * gsw (count x tgsw words, time domain), on `threads` OpenMP threads. */
+void orc_extern_mul_exact_batch(const orc_params* P, int32_t* accum, const int32_t* gsw,
+                                int32_t count, int32_t threads) {
+    const size_t w_acc = (size_t)(P->k + 1) * P->N;
+    const size_t w_gsw = (size_t)(P->k + 1) * P->l * w_acc;
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
+#endif
+    for (int32_t c = 0; c < count; ++c)
+        orc_extern_mul_exact(P, accum + (size_t)c * w_acc, gsw + (size_t)c * w_gsw);
+    (void)threads;
+}
+
+/* Bootstraps without key switch of `count` samples x (count x (n+1)) into
+ * out (count x (kN+1)), exact int64 blind rotation when `exact` (bk in the
+ * time domain), else the FFT blind rotation; on `threads` OpenMP threads. */
+void orc_bootstrap_woks_batch(const orc_params* P, const double* bk_fft, int32_t mu,
+                              const int32_t* x, int32_t* out, int32_t count,
+                              int32_t exact, const int32_t* bk, int32_t threads) {
+    const int32_t w_in = P->n + 1, w_out = P->k * P->N + 1;
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
+#endif
+    for (int32_t c = 0; c < count; ++c)
+        orc_bootstrap_woks(P, bk_fft, mu, x + (size_t)c * w_in, out + (size_t)c * w_out,
+                           exact, bk);
+    (void)threads;
+}
+
+/* Full gates (combine, bootstrap, key switch) with the exact int64 blind
+ * rotation: the exact-product counterpart of orc_boots_gate_batch. */
+void orc_boots_gate_exact_batch(const orc_params* P, const int32_t* bk,
+                                const int32_t* ks, const int32_t* gates,
+                                const int32_t* ca, const int32_t* cb, int32_t* out,
+                                int32_t count, int32_t threads) {
+    const int32_t w = P->n + 1;
+    const int32_t mu = orc_mod_switch_to_torus32(1, 8);
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
+#endif
+    for (int32_t g = 0; g < count; ++g) {
+        std::vector<int32_t> tmp(w), u((size_t)P->k * P->N + 1);
+        orc_gate_combine(P, gates[g], ca + (size_t)g * w, cb + (size_t)g * w, tmp.data());
+        orc_bootstrap_woks(P, nullptr, mu, tmp.data(), u.data(), 1, bk);
+        orc_keyswitch(P, ks, u.data(), out + (size_t)g * w);
+    }
     (void)threads;
 }
 

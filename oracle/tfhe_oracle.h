@@ -152,6 +152,19 @@ void orc_boots_gate_batch(const orc_params* P, const double* bk_fft,
                           const int32_t* ks, const int32_t* gates,
                           const int32_t* ca, const int32_t* cb, int32_t* out,
                           int32_t count, int32_t threads);
+/* independent exact external products (time-domain TGSW per item) */
+void orc_extern_mul_exact_batch(const orc_params* P, int32_t* accum, const int32_t* gsw,
+                                int32_t count, int32_t threads);
+/* bootstraps without key switch of a batch; exact != 0: int64 blind
+ * rotation with the time-domain key bk */
+void orc_bootstrap_woks_batch(const orc_params* P, const double* bk_fft, int32_t mu,
+                              const int32_t* x, int32_t* out, int32_t count,
+                              int32_t exact, const int32_t* bk, int32_t threads);
+/* a batch of gates through the exact int64 blind rotation */
+void orc_boots_gate_exact_batch(const orc_params* P, const int32_t* bk,
+                                const int32_t* ks, const int32_t* gates,
+                                const int32_t* ca, const int32_t* cb, int32_t* out,
+                                int32_t count, int32_t threads);
 int32_t orc_max_threads(void);
 
 #ifdef __cplusplus

@@ -104,6 +104,40 @@ def test_reference_test_bench_against_compat_headers(pkg, oracle, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.skipif(not os.path.isdir(os.path.join(build_ref.REF, "test_bench")),
+                    reason="reference test bench not present (TFHE_REFERENCE_DIR)")
+def test_reference_cloud_runs_its_gates_on_gpu(pkg, tmp_path):
+    """The reference's own test bench end to end with the cloud on the GPU:
+    alice.c, cloud.c and verify.c, unmodified, built against include/tfhe
+    and linked with this library.  alice writes the keys and the two
+    encrypted 16-bit numbers; cloud (cloud.c:39-74) reads them and runs its
+    16 bootsOR calls (cloud.c:58-62) -- each one a gate bootstrap on the GPU,
+    shown by the library's per-call trace -- and writes answer.data; verify
+    decrypts it and prints 499 | 388 = 503."""
+    tb = os.path.join(build_ref.REF, "test_bench")
+    exes = {}
+    for name, rel in (("alice", "client/alice.c"), ("verify", "client/verify.c"), ("cloud", "server/cloud.c")):
+        exes[name] = _build(pkg, os.path.join(tb, rel), str(tmp_path / name))
+    work = tmp_path / "run"
+    (work / "keys").mkdir(parents=True)
+    (work / "data").mkdir()
+    rc, log_a = _run([exes["alice"]], cwd=str(work))
+    assert rc == 0, log_a
+    env = dict(os.environ, TFHE_GB300_TRACE="1")
+    r = subprocess.run([exes["cloud"]], capture_output=True, text=True, cwd=str(work), timeout=600, env=env)
+    log_c = r.stdout + r.stderr
+    assert r.returncode == 0, log_c
+    trace = [ln for ln in log_c.splitlines() if ln.startswith("tfhe_gb300 trace: bootsOR: 1 sample(s) on GPU 0")]
+    assert len(trace) == 16, log_c
+    rc, log_v = _run([exes["verify"]], cwd=str(work))
+    assert rc == 0, log_v
+    print("\n---- alice ----\n" + log_a + "\n---- cloud (TFHE_GB300_TRACE=1) ----\n" + log_c +
+          "\n---- verify ----\n" + log_v)
+    m = re.search(r"And the result is: (-?\d+) vs (\d+)", log_v)
+    assert m and int(m.group(1)) == int(m.group(2)) == (499 | 388), log_v
+
+
+@pytest.mark.gpu
 def test_roundtrip_on_gpu(pkg, tmp_path):
     exe = _build(pkg, os.path.join(HERE, "compat", "roundtrip.c"), str(tmp_path / "roundtrip"))
     for x, y in ((499, 388), (65535, 1), (12345, 54321)):
