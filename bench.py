@@ -775,7 +775,11 @@ def main():
     achieved = FLOP_PER_BOOTSTRAP * batch / (k_ms / 1000.0) / 1e12
     clocks = clk.summary()
     sm_max = clocks.get("sm_max_mhz") or 2070.0
-    peak = SMS * FP32_LANES_PER_SM * 2 * sm_max * 1e6 / 1e12
+    nominal_peak = SMS * FP32_LANES_PER_SM * 2 * sm_max * 1e6 / 1e12
+    # the FP32 FMA-pipe peak measured on this GPU now (packed FMA chains on
+    # every SM; MEASURED_PEAKS.json has no FP32 figure)
+    with ClockSampler(local) as clk_peak:
+        peak, peak_ms = pkg.measure_fp32_peak(local)
 
     extras = {}
     if not args.no_extras and rank == 0:
@@ -837,6 +841,15 @@ def main():
         extras["serving"]["workload"] = ("%d clients x %d requests, Poisson %.1f req/s per client (seed 5), "
                                          "32-bit adders, 16-bit comparators, 8-bit multiplexers, split-FP32"
                                          % (args.clients, args.requests, args.rate))
+        # saturating load: arrivals above the engine's capacity, so the
+        # queue builds up and admission and batching bind
+        reqs, boots = serving_requests(pkg, P, lwe, 64, 32, 50.0, seed=6)
+        sat = run_serving(pkg, eng, P, lwe, reqs, boots, "split_fp32", pool_slots=1 << 20)
+        sat["workload"] = ("64 clients x 32 requests, Poisson 50 req/s per client (seed 6): offered "
+                           "%.0f bootstraps/s, above capacity; pool of 2^20 ciphertext slots, split-FP32"
+                           % (boots / max(r["t"] for r in reqs)))
+        sat["fraction_of_layer_engine"] = sat["bootstraps_per_s"] / value
+        extras["serving_saturated"] = sat
         extras["stress"] = run_stress(torch, pkg, local, args.split_bits)
         cpu = cpu_baseline(args.cpu_seconds, batch)
     else:
@@ -872,8 +885,12 @@ def main():
                          "kernel": " + ".join(blind_rotate_kernels(args.form, eng.get_groups_per_cta(args.form),
                                                                    batch)) + " (blind rotation + extraction)",
                          "kernel_ms": k_ms,
-                         "peak_source": "nominal FP32 pipe: 152 SMs x 128 lanes x 2 x max SM clock "
-                                        "(no measured FP32 peak in MEASURED_PEAKS.json)"},
+                         "peak_source": "measured in this run: tfhe_gpu_measure_fp32_peak (independent packed "
+                                        "FP32 FMA chains on every SM, CUDA events, %.1f ms; SM clock %s MHz); "
+                                        "MEASURED_PEAKS.json has no FP32 figure" % (peak_ms,
+                                                                                     clk_peak.summary().get("sm_mhz")),
+                         "nominal_peak": nominal_peak,
+                         "frac_of_nominal": achieved / nominal_peak},
             "clocks": clocks,
         }
         line.update(extras)

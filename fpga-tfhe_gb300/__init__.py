@@ -57,6 +57,15 @@ class Params(ctypes.Structure):
         return self.k * self.N * self.ks_t * (1 << self.ks_basebit) * (self.n + 1)
 
 
+def measure_fp32_peak(device=0, iters=65536):
+    """Measured FP32 FMA-pipe peak of the device: (TFLOP/s, probe ms)."""
+    tf, ms = ctypes.c_double(), ctypes.c_double()
+    st = lib().tfhe_gpu_measure_fp32_peak(int(device), int(iters), ctypes.byref(tf), ctypes.byref(ms))
+    if st:
+        raise TfheError(st, "measure_fp32_peak")
+    return tf.value, ms.value
+
+
 def default_params():
     """The reference's default gate set (constants.h:26-40)."""
     return Params(n=630, N=1024, k=1, l=3, Bgbit=7, ks_t=8, ks_basebit=2, split_bits=0,
@@ -151,6 +160,9 @@ SIGNATURES = {
     "tfhe_client_test_vector": (ctypes.c_int, [ctypes.c_int32, I32P, ctypes.c_int32, I32P]),
     "tfhe_gpu_gate_keyset": (ctypes.c_int, [VP, I32P, I32P, I32P, I32P, ctypes.c_uint32]),
     "tfhe_gpu_selftest_timeout": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int32]),
+    "tfhe_gpu_measure_fp32_peak": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32,
+                                                  ctypes.POINTER(ctypes.c_double),
+                                                  ctypes.POINTER(ctypes.c_double)]),
     "tfhe_client_set_seed": (None, [U32P, ctypes.c_int32]),
     "tfhe_client_gate_keyset": (ctypes.c_int, [ctypes.c_void_p, I32P, I32P, I32P, I32P]),
     "tfhe_client_encrypt_bits": (ctypes.c_int, [ctypes.c_void_p, I32P, ctypes.c_int32, I32P, I32P]),
@@ -488,7 +500,9 @@ class Engine:
         split_fp32: 0 automatic; 1, 2, 4 L2-direct; 5-8 shared key ring, one
         transform at a time; 9 ring, 4 per CTA, a step's transforms
         together; 10 ring, 6 per CTA, two at a time; 11-13 pair kernel;
-        14 spread kernel (lowest latency).  fp64: 3 or 4."""
+        14 spread kernel (lowest latency); 15 automatic in fixed summation
+        order (no pair kernel: results independent of the batch).  fp64: 3
+        or 4."""
         self._check(self.lib.tfhe_gpu_set_groups_per_cta(self.ctx, self._form(form), int(groups)),
                     "set_groups_per_cta")
 

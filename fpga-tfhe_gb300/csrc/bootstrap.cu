@@ -1582,8 +1582,15 @@ cudaError_t launch_ring_pairs(const DevParams& P, const Tables& T, const EpArgs&
 // SM; a remainder of at most 1 per SM on the spread kernel, of 2 per SM on
 // the pair kernel, of at most 4 per SM as one launch_ring_batched wave, else
 // one more 6-per-SM wave.
+//
+// fixed_order (shape 15): the pair kernel, which adds its two halves' partial
+// products and so may round differently, is replaced by the spread kernel
+// (two waves for 2 per SM, 3.8 ms against 3.3 ms): every launch then sums
+// the 2l key rows in the same order, and a ciphertext's result does not
+// depend on the batch it runs in -- what a server that mixes requests needs.
 template <int L>
-cudaError_t launch_auto_fp32(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
+cudaError_t launch_auto_fp32(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st,
+                             bool fixed_order = false) {
     const int wave = 6 * kSmCount;
     const int full = (a.count / wave) * wave;
     const int rest = a.count - full;
@@ -1594,7 +1601,7 @@ cudaError_t launch_auto_fp32(const DevParams& P, const Tables& T, const EpArgs& 
     }
     const EpArgs tail = slice_blind_rotate(P, a, full, rest);
     if (rest > 2 * kSmCount) return launch_ring_batched<L>(P, T, tail, st);
-    if (rest > kSmCount) return launch_pair_fp32<L>(P, T, tail, 2, st);
+    if (rest > kSmCount && !fixed_order) return launch_pair_fp32<L>(P, T, tail, 2, st);
     return launch_spread<L>(P, T, tail, st);
 }
 
@@ -1617,11 +1624,13 @@ cudaError_t launch_ep_l(const DevParams& P, Form f, EpMode mode, const Tables& T
     case kEpMuxRotate: return launch_ep_t<float, 2, kEpMuxRotate, 4, L>(P, T, a, st);
     default:
         if (groups == 0) return launch_auto_fp32<L>(P, T, a, st);
+        if (groups == 15) return launch_auto_fp32<L>(P, T, a, st, true);
         // 1, 2, 4: L2-direct key reads; 5: shared ring fed by a producer
         // warp; 6, 7, 8: shared ring fed in line by one consumer thread;
         // 9: shared ring, 4 per CTA, a step's l forward transforms run
         // together; 10: shared ring, 6 per CTA, transforms two at a time;
-        // 11, 12, 13: pair kernel with 1, 2, 3 ciphertexts per CTA
+        // 11, 12, 13: pair kernel with 1, 2, 3 ciphertexts per CTA;
+        // 15: the automatic shape in fixed summation order (no pair kernel)
         if (groups >= 11 && groups <= 13) return launch_pair_fp32<L>(P, T, a, groups - 10, st);
         if (groups == 9) return launch_ring_batched<L>(P, T, a, st);
         if (groups == 10) return launch_ring_pairs<L>(P, T, a, st);
@@ -1742,7 +1751,7 @@ cudaError_t launch_engine64_to_lagrange_ref(const void* eng, double* ref, int np
 int blind_rotate_tail_start(Form f, int groups, int count) {
     // launch_auto_fp32's split: whole 6-per-SM waves, then a remainder of
     // at most 4 per SM that runs as its own launch on part of the SMs
-    if (f != kFormSplitFp32 || groups != 0) return 0;
+    if (f != kFormSplitFp32 || (groups != 0 && groups != 15)) return 0;
     const int wave = 6 * kSmCount;
     const int full = (count / wave) * wave;
     const int rest = count - full;

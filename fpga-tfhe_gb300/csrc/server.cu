@@ -6,20 +6,36 @@
 // server as a request loop: many clients submit circuits (gate lists over
 // their input ciphertexts); the server keeps every admitted circuit's wires
 // resident in a device ciphertext pool, and each tick runs, as one batch,
-// every gate of every admitted circuit whose inputs are ready.  New circuits
-// are admitted between ticks as pool slots free up (admission by device
-// memory), so their first layer shares a launch with other circuits' later
-// layers.  Results are bit-identical whatever the batch composition: each
-// ciphertext's bootstrap is computed independently of its neighbours.
+// every gate of every admitted circuit whose inputs are available.  New
+// circuits are admitted between ticks as pool slots free up (admission by
+// device memory), so their first layer shares a launch with other circuits'
+// later layers.  Results are bit-identical whatever the batch composition:
+// each ciphertext's bootstrap is computed independently of its neighbours.
+//
+// Pipelining.  Ticks run in order on the context's stream, so a tick may use
+// the outputs of the tick before it without the host waiting for them: a
+// gate is schedulable as soon as all its inputs are scheduled.  The host
+// builds and enqueues tick k + 1 (admission, readiness, index staging) while
+// tick k runs on the device; at most two ticks are in flight, each with its
+// own pinned staging buffers.  Readiness is incremental: every gate counts
+// its unscheduled inputs and joins the ready queue when the count reaches
+// zero, so a tick costs time in proportion to the gates it schedules, not to
+// the gates of all active circuits.  A tick's completion is observed through
+// its events: the first step() that finds them complete retires the tick --
+// latencies from the device timestamps, outputs of the circuits it finished
+// (gathered on the device and copied back in one transfer inside the tick),
+// pool slots freed -- so one retire handles any number of circuits.
 //
 // Gates: the ten two-input bootstrapped gates (tfhe_gpu_gate ids 0..9), MUX
 // (id 10, upstream bootsMUX: two bootstraps without key switch, one key
 // switch), NOT (11) and COPY (12) without bootstrapping, CONSTANT (13, in0 =
 // the bit).  Wire ids: [0, ninputs) are the circuit's inputs, ninputs + g is
 // the output of gate g; gates must be listed in an order where each gate's
-// inputs come earlier.
+// inputs come earlier.  NOT / COPY / CONSTANT run at the start of a tick, in
+// levels, so bootstrapped gates of the same tick may read them.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <deque>
@@ -92,9 +108,14 @@ int grid_for(size_t total) {
     return (int)(b > 8192 ? 8192 : (b < 1 ? 1 : b));
 }
 
+constexpr int kInFlight = 2;  // ticks in flight (staging buffers)
+
 struct Gate {
     int32_t type, in[3];
 };
+
+int n_inputs(int32_t type) { return type == 10 ? 3 : (type <= 9 ? 2 : (type == 13 ? 0 : 1)); }
+bool is_linear(int32_t type) { return type >= 11; }
 
 struct Circuit {
     int64_t id;
@@ -103,14 +124,39 @@ struct Circuit {
     std::vector<int32_t> outputs;        // wire ids
     std::vector<int32_t> input_ct;       // host copy until admitted
     std::vector<int32_t> slot;           // wire -> pool slot
-    std::vector<char> ready;             // wire ready
-    std::vector<char> done;              // gate done
-    std::vector<char> queued;            // gate in the ready list
-    std::vector<double> ready_at;        // gate became ready (s)
-    int32_t remaining = 0;
+    // readiness: users of each wire (CSR over wires), unscheduled inputs per gate
+    std::vector<int32_t> user_off, users;
+    std::vector<int32_t> pending;
+    std::vector<int64_t> wire_tick;      // tick that produces the wire (-1: an input)
+    std::vector<int8_t> wire_level;      // linear level within that tick (-1: a bootstrap)
+    std::vector<double> produced;        // device completion time of the wire (s)
+    int32_t unscheduled = 0;             // gates not yet in a tick
     double submitted = 0, admitted = 0, finished = 0;
     std::vector<int32_t> result;         // host result when finished
-    bool is_done = false;
+};
+
+struct Pick {
+    Circuit* c;
+    int32_t g;
+};
+
+// One tick: what it runs, what it finishes, its events and staging.
+struct Tick {
+    int64_t index = -1;
+    bool busy = false;                          // enqueued, not yet retired
+    std::vector<std::vector<Pick>> lin;         // linear gates by level
+    std::vector<Pick> boot, mux;
+    std::vector<Circuit*> finishing;            // circuits whose last gates are in this tick
+    std::vector<int32_t> finishing_off;         // their first row in the result buffer
+    cudaEvent_t start = nullptr, end = nullptr;
+    int32_t* h_stage = nullptr;                 // pinned: indices, gate ids, uploads
+    size_t h_stage_words = 0;
+    int32_t* d_stage = nullptr;                 // device copy of h_stage
+    size_t d_stage_words = 0;
+    int32_t* h_res = nullptr;                   // pinned: finished circuits' outputs
+    size_t h_res_words = 0;
+    int32_t* d_res = nullptr;                   // device gather of those outputs
+    size_t d_res_words = 0;
 };
 
 }  // namespace
@@ -129,17 +175,20 @@ struct tfhe_gpu_server {
     int32_t* d_u = nullptr;       // max_batch x ext_width: extracted samples
     int32_t* d_s = nullptr;       // max_batch/2 x ext_width: MUX sums
     int32_t* d_out = nullptr;     // max_batch x width: key-switched outputs
-    int32_t* d_gates = nullptr;   // max_batch gate ids of the bootstraps
-    int32_t* d_idx = nullptr;     // 3 x max_batch (a slots, b slots, destination slots)
-    int32_t* d_lin = nullptr;     // 3 x max_batch
-    int32_t* h_idx = nullptr;     // pinned staging, 4 x max_batch
     std::vector<int32_t> free_slots;
     std::deque<std::unique_ptr<Circuit>> waiting;
     std::map<int64_t, std::unique_ptr<Circuit>> active;
     std::map<int64_t, std::unique_ptr<Circuit>> finished;
+    std::deque<Pick> ready;                     // schedulable gates, in order of readiness
+    std::vector<Circuit*> admitted_now;         // inputs to upload with the next tick
+    Tick ticks[kInFlight];
+    int64_t next_tick = 0;                      // index of the next tick to enqueue
+    int64_t next_retire = 0;                    // index of the oldest tick not retired
+    cudaEvent_t epoch = nullptr;                // device time origin
+    double epoch_host = 0;
     int64_t next_id = 1;
     // statistics
-    std::vector<double> gate_latency;   // per bootstrapped gate: ready -> done (s)
+    std::vector<double> gate_latency;   // per bootstrapped gate: inputs available -> done (s)
     std::vector<double> request_latency;
     int64_t gates_run = 0;
     double busy_s = 0;
@@ -161,11 +210,103 @@ tfhe_gpu_status srv_fail(tfhe_gpu_server* s, tfhe_gpu_status st, const std::stri
                             std::string(#expr) + ": " + cudaGetErrorString(e_));           \
     } while (0)
 
-bool is_boot(int32_t t) { return t >= 0 && t <= 10; }
+// grow a pinned host buffer (only while no transfer uses it)
+cudaError_t grow_host(int32_t** p, size_t* have, size_t need) {
+    if (need <= *have) return cudaSuccess;
+    if (*p) cudaFreeHost(*p);
+    *p = nullptr;
+    *have = 0;
+    size_t cap = std::max(need, (size_t)1 << 16);
+    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(p), cap * sizeof(int32_t), cudaHostAllocDefault);
+    if (e == cudaSuccess) *have = cap;
+    return e;
+}
+
+// grow a device buffer (only while no kernel uses it)
+cudaError_t grow_dev(int32_t** p, size_t* have, size_t need) {
+    if (need <= *have) return cudaSuccess;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    size_t cap = std::max(need, (size_t)1 << 16);
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), cap * sizeof(int32_t));
+    if (e == cudaSuccess) *have = cap;
+    return e;
+}
+
+double device_time(tfhe_gpu_server* s, cudaEvent_t ev) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, s->epoch, ev);
+    return s->epoch_host + 1e-3 * ms;
+}
+
+// the gate's output wire is scheduled: its users lose one pending input
+template <typename F>
+void release_users(Circuit* c, int32_t g, F&& on_ready) {
+    const int32_t w = c->ninputs + g;
+    for (int32_t i = c->user_off[w]; i < c->user_off[w + 1]; ++i) {
+        const int32_t u = c->users[i];
+        if (--c->pending[u] == 0) on_ready(u);
+    }
+}
+
+// Retire the oldest in-flight tick (its events have completed): device
+// completion time, latencies, wire availability times, finished circuits.
+tfhe_gpu_status retire_tick(tfhe_gpu_server* s, Tick& T) {
+    const double t_end = device_time(s, T.end);
+    float busy_ms = 0.f;
+    cudaEventElapsedTime(&busy_ms, T.start, T.end);
+    s->busy_s += 1e-3 * busy_ms;
+    auto avail = [&](const Circuit* c, const Gate& G) {
+        double r = c->admitted;
+        for (int k = 0; k < n_inputs(G.type); ++k) r = std::max(r, c->produced[G.in[k]]);
+        return r;
+    };
+    for (auto& level : T.lin)  // levels in order: a linear output is available with its inputs
+        for (const Pick& p : level) p.c->produced[p.c->ninputs + p.g] = avail(p.c, p.c->gates[p.g]);
+    for (auto* list : {&T.boot, &T.mux})
+        for (const Pick& p : *list) {
+            record(s->gate_latency, t_end - avail(p.c, p.c->gates[p.g]));
+            p.c->produced[p.c->ninputs + p.g] = t_end;
+        }
+    const int32_t W = s->width;
+    for (size_t i = 0; i < T.finishing.size(); ++i) {
+        Circuit* c = T.finishing[i];
+        c->result.assign(T.h_res + (size_t)T.finishing_off[i] * W,
+                         T.h_res + (size_t)(T.finishing_off[i] + c->outputs.size()) * W);
+        for (int32_t sl : c->slot) s->free_slots.push_back(sl);
+        c->finished = t_end;
+        record(s->request_latency, c->finished - c->submitted);
+        auto it = s->active.find(c->id);
+        s->finished[c->id] = std::move(it->second);
+        s->active.erase(it);
+    }
+    T.lin.clear();
+    T.boot.clear();
+    T.mux.clear();
+    T.finishing.clear();
+    T.finishing_off.clear();
+    T.busy = false;
+    ++s->next_retire;
+    return TFHE_GPU_OK;
+}
+
+// Retire completed ticks in order; with `wait`, block for the oldest one.
+tfhe_gpu_status retire(tfhe_gpu_server* s, bool wait) {
+    while (s->next_retire < s->next_tick) {
+        Tick& T = s->ticks[s->next_retire % kInFlight];
+        cudaError_t e = wait ? cudaEventSynchronize(T.end) : cudaEventQuery(T.end);
+        if (e == cudaErrorNotReady) return TFHE_GPU_OK;
+        SCK(s, e);
+        tfhe_gpu_status st = retire_tick(s, T);
+        if (st != TFHE_GPU_OK) return st;
+        wait = false;
+    }
+    return TFHE_GPU_OK;
+}
 
 // admit waiting circuits while their wires fit in the pool
-tfhe_gpu_status admit(tfhe_gpu_server* s) {
-    cudaStream_t st = s->ctx->stream;
+void admit(tfhe_gpu_server* s) {
     while (!s->waiting.empty()) {
         Circuit* c = s->waiting.front().get();
         const size_t need = c->slot.size();
@@ -174,17 +315,212 @@ tfhe_gpu_status admit(tfhe_gpu_server* s) {
             c->slot[w] = s->free_slots.back();
             s->free_slots.pop_back();
         }
-        // upload inputs (one copy per input; inputs are contiguous on the host)
-        for (int32_t i = 0; i < c->ninputs; ++i) {
-            SCK(s, cudaMemcpyAsync(s->d_pool + (size_t)c->slot[i] * s->width,
-                                   c->input_ct.data() + (size_t)i * s->width,
-                                   sizeof(int32_t) * s->width, cudaMemcpyHostToDevice, st));
-            c->ready[i] = 1;
-        }
         c->admitted = now_s();
+        for (int32_t g = 0; g < (int32_t)c->gates.size(); ++g)
+            if (c->pending[g] == 0) s->ready.push_back({c, g});
+        s->admitted_now.push_back(c);
         s->active[c->id] = std::move(s->waiting.front());
         s->waiting.pop_front();
     }
+}
+
+// Choose the gates of tick k from the ready queue.
+void schedule(tfhe_gpu_server* s, Tick& T, int64_t k) {
+    std::deque<Pick> keep, next;
+    int32_t slots = 0;  // bootstraps in this tick
+    while (!s->ready.empty()) {
+        const Pick p = s->ready.front();
+        s->ready.pop_front();
+        Circuit* c = p.c;
+        const Gate& G = c->gates[p.g];
+        const int32_t out = c->ninputs + p.g;
+        if (is_linear(G.type)) {
+            int lvl = 0;
+            for (int q = 0; q < n_inputs(G.type); ++q) {
+                const int32_t w = G.in[q];
+                if (c->wire_tick[w] == k && c->wire_level[w] >= 0) lvl = std::max(lvl, c->wire_level[w] + 1);
+            }
+            if ((int)T.lin.size() <= lvl) T.lin.resize(lvl + 1);
+            T.lin[lvl].push_back(p);
+            c->wire_tick[out] = k;
+            c->wire_level[out] = (int8_t)std::min(lvl, 127);
+            // a linear output is available within the tick
+            release_users(c, p.g, [&](int32_t u) { s->ready.push_back({c, u}); });
+        } else {
+            const int need = G.type == 10 ? 2 : 1;
+            if (slots + need > s->max_batch) {
+                keep.push_back(p);
+                continue;
+            }
+            slots += need;
+            (G.type == 10 ? T.mux : T.boot).push_back(p);
+            c->wire_tick[out] = k;
+            c->wire_level[out] = -1;
+            // a bootstrap's output is available to the next tick
+            release_users(c, p.g, [&](int32_t u) { next.push_back({c, u}); });
+        }
+        if (--c->unscheduled == 0) T.finishing.push_back(c);
+    }
+    s->ready = std::move(keep);
+    for (const Pick& p : next) s->ready.push_back(p);
+}
+
+// Enqueue tick T: uploads of newly admitted circuits, linear levels, the
+// bootstraps, scatter, the finished circuits' outputs back to the host.
+tfhe_gpu_status enqueue(tfhe_gpu_server* s, Tick& T) {
+    tfhe_gpu_ctx* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    const int32_t W = s->width, EW = s->ext_width;
+    // staging layout (int32 words): [upload slots][linear ops 3 x nl]
+    // [a, b, destination slots 3 x nb][gate ids nb][result slots][upload ciphertexts]
+    size_t n_up = 0;
+    for (Circuit* c : s->admitted_now) n_up += c->ninputs;
+    size_t nl = 0;
+    for (auto& level : T.lin) nl += level.size();
+    const int32_t nr = (int32_t)T.boot.size(), nm = (int32_t)T.mux.size();
+    const int32_t nb = nr + 2 * nm;
+    size_t n_res = 0;
+    for (Circuit* c : T.finishing) {
+        T.finishing_off.push_back((int32_t)n_res);
+        n_res += c->outputs.size();
+    }
+    const size_t o_lin = n_up, o_idx = o_lin + 3 * nl, o_gid = o_idx + 3 * (size_t)nb;
+    const size_t o_res = o_gid + nb, o_ct = o_res + n_res;
+    const size_t words = o_ct + n_up * W;
+    SCK(s, grow_host(&T.h_stage, &T.h_stage_words, words));
+    SCK(s, grow_dev(&T.d_stage, &T.d_stage_words, words));
+    SCK(s, grow_host(&T.h_res, &T.h_res_words, n_res * W));
+    SCK(s, grow_dev(&T.d_res, &T.d_res_words, n_res * W));
+    int32_t* h = T.h_stage;
+    {
+        size_t i = 0;
+        for (Circuit* c : s->admitted_now) {
+            for (int32_t q = 0; q < c->ninputs; ++q) h[i + q] = c->slot[q];
+            std::memcpy(h + o_ct + i * W, c->input_ct.data(), sizeof(int32_t) * (size_t)c->ninputs * W);
+            i += c->ninputs;
+            c->input_ct.clear();
+            c->input_ct.shrink_to_fit();
+        }
+    }
+    {
+        size_t i = 0;
+        for (auto& level : T.lin)
+            for (const Pick& p : level) {
+                const Gate& G = p.c->gates[p.g];
+                h[o_lin + 3 * i] = p.c->slot[p.c->ninputs + p.g];
+                h[o_lin + 3 * i + 1] = G.type == 13 ? -1 : p.c->slot[G.in[0]];
+                h[o_lin + 3 * i + 2] = G.type == 12 ? 0 : (G.type == 11 ? 1 : (G.in[0] ? 2 : 3));
+                ++i;
+            }
+    }
+    // bootstraps: [plain gates | MUX first halves AND(a, b) | MUX second
+    // halves ANDNY(a, c)]; the MUX halves are summed with (0, 1/8) before
+    // their key switch (upstream bootsMUX)
+    int32_t* ha = h + o_idx;
+    int32_t* hb = ha + nb;
+    int32_t* hd = hb + nb;
+    int32_t* hg = h + o_gid;
+    for (int32_t i = 0; i < nr; ++i) {
+        const Pick& p = T.boot[i];
+        const Gate& G = p.c->gates[p.g];
+        ha[i] = p.c->slot[G.in[0]];
+        hb[i] = p.c->slot[G.in[1]];
+        hg[i] = G.type;
+        hd[i] = p.c->slot[p.c->ninputs + p.g];
+    }
+    for (int32_t j = 0; j < nm; ++j) {
+        const Pick& p = T.mux[j];
+        const Gate& G = p.c->gates[p.g];
+        const int32_t* sl = p.c->slot.data();
+        ha[nr + j] = sl[G.in[0]];
+        hb[nr + j] = sl[G.in[1]];
+        hg[nr + j] = TFHE_GATE_AND;
+        ha[nr + nm + j] = sl[G.in[0]];
+        hb[nr + nm + j] = sl[G.in[2]];
+        hg[nr + nm + j] = TFHE_GATE_ANDNY;
+        hd[nr + j] = sl[p.c->ninputs + p.g];
+    }
+    {
+        size_t i = 0;
+        for (Circuit* c : T.finishing)
+            for (int32_t w : c->outputs) h[o_res + i++] = c->slot[w];
+    }
+    s->admitted_now.clear();
+
+    SCK(s, cudaEventRecord(T.start, st));
+    SCK(s, cudaMemcpyAsync(T.d_stage, h, sizeof(int32_t) * words, cudaMemcpyHostToDevice, st));
+    const int32_t* d = T.d_stage;
+    if (n_up) {
+        k_scatter<<<grid_for(n_up * W), 256, 0, st>>>(d + o_ct, d, s->d_pool, W, (int)n_up);
+        SCK(s, cudaGetLastError());
+    }
+    {
+        size_t off = 0;
+        for (auto& level : T.lin) {
+            k_linear<<<grid_for(level.size() * W), 256, 0, st>>>(s->d_pool, d + o_lin + 3 * off, W,
+                                                                 (int)level.size());
+            SCK(s, cudaGetLastError());
+            off += level.size();
+        }
+    }
+    if (nb > 0) {
+        const int grid = grid_for((size_t)nb * W);
+        k_gather<<<grid, 256, 0, st>>>(s->d_pool, d + o_idx, s->d_a, W, nb);
+        k_gather<<<grid, 256, 0, st>>>(s->d_pool, d + o_idx + nb, s->d_b, W, nb);
+        SCK(s, cudaGetLastError());
+        SCK(s, launch_gate_combine(ctx->dp, d + o_gid, 0, s->d_a, s->d_b, s->d_x, nb, st));
+        EpArgs a{};
+        a.err = ctx->d_err;
+        a.mu = 1 << 29;
+        a.gsw = ctx->d_bk[s->form];
+        // the automatic split-FP32 shape in its fixed summation order, so a
+        // circuit's ciphertexts do not depend on the requests it shares
+        // ticks with
+        const int groups = s->form == TFHE_GPU_SPLIT_FP32 && ctx->groups_per_cta[s->form] == 0
+                               ? 15 : ctx->groups_per_cta[s->form];
+        // As in a gate batch: when the blind rotation splits into full waves
+        // and a remainder wave on part of the SMs, the full waves' plain-gate
+        // key switch runs on the side stream during the remainder.
+        const int split = blind_rotate_tail_start((Form)s->form, groups, nb);
+        const int k1 = std::min(split, nr);
+        auto rotate = [&](int off, int cnt) -> cudaError_t {
+            EpArgs b = a;
+            b.x = s->d_x + (size_t)off * W;
+            b.lwe_out = s->d_u + (size_t)off * EW;
+            b.count = cnt;
+            return launch_external_product(ctx->dp, (Form)s->form, kEpBlindRotate, ctx->tables, b,
+                                           groups, st);
+        };
+        SCK(s, rotate(0, split ? split : nb));
+        if (split && k1 > 0) {
+            SCK(s, cudaEventRecord(ctx->ev_fork, st));
+            SCK(s, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+            SCK(s, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, s->d_u, s->d_out, k1, ctx->side));
+            SCK(s, cudaEventRecord(ctx->ev_join, ctx->side));
+        }
+        if (split) SCK(s, rotate(split, nb - split));
+        const int k0 = split && k1 > 0 ? k1 : 0;
+        SCK(s, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, s->d_u + (size_t)k0 * EW,
+                                s->d_out + (size_t)k0 * W, nr - k0, st));
+        if (nm) {
+            SCK(s, launch_lwe_add2_const(s->d_u + (size_t)nr * EW, s->d_u + (size_t)(nr + nm) * EW,
+                                         s->d_s, EW, 1 << 29, nm, st));
+            SCK(s, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, s->d_s,
+                                    s->d_out + (size_t)nr * W, nm, st));
+        }
+        if (split && k1 > 0) SCK(s, cudaStreamWaitEvent(st, ctx->ev_join, 0));
+        k_scatter<<<grid_for((size_t)(nr + nm) * W), 256, 0, st>>>(s->d_out, d + o_idx + 2 * nb, s->d_pool,
+                                                                     W, nr + nm);
+        SCK(s, cudaGetLastError());
+    }
+    if (n_res) {
+        k_gather<<<grid_for(n_res * W), 256, 0, st>>>(s->d_pool, d + o_res, T.d_res, W, (int)n_res);
+        SCK(s, cudaGetLastError());
+        SCK(s, cudaMemcpyAsync(T.h_res, T.d_res, sizeof(int32_t) * n_res * W, cudaMemcpyDeviceToHost, st));
+    }
+    SCK(s, cudaEventRecord(T.end, st));
+    T.busy = true;
+    s->gates_run += nb;
     return TFHE_GPU_OK;
 }
 
@@ -194,7 +530,7 @@ extern "C" {
 
 tfhe_gpu_status tfhe_gpu_server_create(tfhe_gpu_ctx* ctx, int32_t pool_slots, int32_t max_batch,
                                        tfhe_gpu_form form, tfhe_gpu_server** out) {
-    if (!ctx || !out || pool_slots < 4 || max_batch < 1 ||
+    if (!ctx || !out || pool_slots < 4 || max_batch < 2 ||
         (form != TFHE_GPU_FP64 && form != TFHE_GPU_SPLIT_FP32))
         return TFHE_GPU_BAD_PARAM;
     *out = nullptr;
@@ -215,10 +551,12 @@ tfhe_gpu_status tfhe_gpu_server_create(tfhe_gpu_ctx* ctx, int32_t pool_slots, in
               cudaMalloc(&s->d_u, ew * max_batch) == cudaSuccess &&
               cudaMalloc(&s->d_s, ew * (max_batch / 2 + 1)) == cudaSuccess &&
               cudaMalloc(&s->d_out, lw * max_batch) == cudaSuccess &&
-              cudaMalloc(&s->d_gates, sizeof(int32_t) * max_batch) == cudaSuccess &&
-              cudaMalloc(&s->d_idx, sizeof(int32_t) * 3 * max_batch) == cudaSuccess &&
-              cudaMalloc(&s->d_lin, sizeof(int32_t) * 3 * max_batch) == cudaSuccess &&
-              cudaMallocHost(&s->h_idx, sizeof(int32_t) * 4 * max_batch) == cudaSuccess;
+              cudaEventCreate(&s->epoch) == cudaSuccess;
+    for (Tick& T : s->ticks)
+        ok = ok && cudaEventCreate(&T.start) == cudaSuccess && cudaEventCreate(&T.end) == cudaSuccess;
+    if (ok) ok = cudaEventRecord(s->epoch, ctx->stream) == cudaSuccess &&
+                 cudaEventSynchronize(s->epoch) == cudaSuccess;
+    s->epoch_host = now_s();
     if (!ok) {
         tfhe_gpu_server_destroy(s);
         return TFHE_GPU_OOM;
@@ -233,6 +571,7 @@ void tfhe_gpu_server_destroy(tfhe_gpu_server* s) {
     if (!s) return;
     cudaSetDevice(s->ctx->device);
     cudaStreamSynchronize(s->ctx->stream);
+    cudaStreamSynchronize(s->ctx->side);
     cudaFree(s->d_pool);
     cudaFree(s->d_a);
     cudaFree(s->d_b);
@@ -240,10 +579,15 @@ void tfhe_gpu_server_destroy(tfhe_gpu_server* s) {
     cudaFree(s->d_u);
     cudaFree(s->d_s);
     cudaFree(s->d_out);
-    cudaFree(s->d_gates);
-    cudaFree(s->d_idx);
-    cudaFree(s->d_lin);
-    if (s->h_idx) cudaFreeHost(s->h_idx);
+    for (Tick& T : s->ticks) {
+        if (T.start) cudaEventDestroy(T.start);
+        if (T.end) cudaEventDestroy(T.end);
+        if (T.h_stage) cudaFreeHost(T.h_stage);
+        if (T.h_res) cudaFreeHost(T.h_res);
+        cudaFree(T.d_stage);
+        cudaFree(T.d_res);
+    }
+    if (s->epoch) cudaEventDestroy(s->epoch);
     delete s;
 }
 
@@ -262,185 +606,80 @@ tfhe_gpu_status tfhe_gpu_server_submit(tfhe_gpu_server* s, const int32_t* gates,
     if (nwires > s->pool_slots)
         return srv_fail(s, TFHE_GPU_BAD_PARAM, "circuit has more wires than the pool has slots");
     auto c = std::make_unique<Circuit>();
-    c->id = s->next_id++;
     c->ninputs = ninputs;
     c->gates.resize(ngates);
+    c->pending.assign(ngates, 0);
+    std::vector<int32_t> nuse(nwires + 1, 0);
     for (int32_t g = 0; g < ngates; ++g) {
         Gate& G = c->gates[g];
         G.type = gates[4 * g];
         for (int k = 0; k < 3; ++k) G.in[k] = gates[4 * g + 1 + k];
-        const int nin = G.type == 10 ? 3 : (G.type <= 9 ? 2 : (G.type == 13 ? 0 : 1));
         if (G.type < 0 || G.type > 13) return srv_fail(s, TFHE_GPU_BAD_PARAM, "unknown gate type");
-        for (int k = 0; k < nin; ++k)
+        for (int k = 0; k < n_inputs(G.type); ++k) {
             if (G.in[k] < 0 || G.in[k] >= ninputs + g)
                 return srv_fail(s, TFHE_GPU_BAD_PARAM, "gate input must be an earlier wire");
+            if (G.in[k] >= ninputs) {  // another gate's output: pending until it is scheduled
+                ++c->pending[g];
+                ++nuse[G.in[k]];
+            }
+        }
     }
+    if (ngates == 0)
+        return srv_fail(s, TFHE_GPU_BAD_PARAM, "circuit has no gates (its outputs are its inputs)");
     for (int32_t o = 0; o < noutputs; ++o)
         if (output_wires[o] < 0 || output_wires[o] >= nwires)
             return srv_fail(s, TFHE_GPU_BAD_PARAM, "bad output wire");
+    c->user_off.assign(nwires + 1, 0);
+    for (int32_t w = 0; w < nwires; ++w) c->user_off[w + 1] = c->user_off[w] + nuse[w];
+    c->users.resize(c->user_off[nwires]);
+    std::vector<int32_t> fill(c->user_off.begin(), c->user_off.end() - 1);
+    for (int32_t g = 0; g < ngates; ++g)
+        for (int k = 0; k < n_inputs(c->gates[g].type); ++k)
+            if (c->gates[g].in[k] >= ninputs) c->users[fill[c->gates[g].in[k]]++] = g;
+    c->id = s->next_id++;
     c->outputs.assign(output_wires, output_wires + noutputs);
     c->input_ct.assign(input_ct, input_ct + (size_t)ninputs * s->width);
     c->slot.assign(nwires, -1);
-    c->ready.assign(nwires, 0);
-    c->done.assign(ngates, 0);
-    c->queued.assign(ngates, 0);
-    c->ready_at.assign(ngates, 0.0);
-    c->remaining = ngates;
+    c->wire_tick.assign(nwires, -1);
+    c->wire_level.assign(nwires, -1);
+    c->produced.assign(nwires, 0.0);
+    c->unscheduled = ngates;
     c->submitted = now_s();
     *request_id = c->id;
     s->waiting.push_back(std::move(c));
     return TFHE_GPU_OK;
 }
 
-// One scheduling tick: admit circuits that fit, run every ready gate of every
-// admitted circuit (up to max_batch bootstraps) as one batch, retire finished
-// circuits.  *ran = number of gates executed (0 when idle).
+// One tick: retire completed ticks, admit circuits that fit, schedule every
+// schedulable gate (up to max_batch bootstraps) and enqueue it as one batch
+// without waiting for the device.  With two ticks already in flight it first
+// waits for the older; with nothing to schedule it waits for the oldest tick
+// in flight, so a loop of steps makes progress.  *ran = gates enqueued.
 tfhe_gpu_status tfhe_gpu_server_step(tfhe_gpu_server* s, int32_t* ran) {
     if (!s) return TFHE_GPU_BAD_PARAM;
     if (ran) *ran = 0;
     if (cudaSetDevice(s->ctx->device) != cudaSuccess) return TFHE_GPU_DEVICE_ERROR;
-    tfhe_gpu_status st0 = admit(s);
-    if (st0 != TFHE_GPU_OK) return st0;
-    cudaStream_t st = s->ctx->stream;
-    const double t0 = now_s();
-    // collect ready gates
-    struct Pick {
-        Circuit* c;
-        int32_t g;
-    };
-    std::vector<Pick> boot, mux, lin;
-    for (auto& kv : s->active) {
-        Circuit* c = kv.second.get();
-        for (int32_t g = 0; g < (int32_t)c->gates.size(); ++g) {
-            if (c->done[g]) continue;
-            const Gate& G = c->gates[g];
-            const int nin = G.type == 10 ? 3 : (G.type <= 9 ? 2 : (G.type == 13 ? 0 : 1));
-            bool rdy = true;
-            for (int k = 0; k < nin; ++k) rdy = rdy && c->ready[G.in[k]];
-            if (!rdy) continue;
-            if (!c->queued[g]) {
-                c->queued[g] = 1;
-                c->ready_at[g] = t0;
-            }
-            if (G.type <= 9) {
-                if ((int32_t)(boot.size() + 2 * mux.size()) + 1 <= s->max_batch) boot.push_back({c, g});
-            } else if (G.type == 10) {
-                if ((int32_t)(boot.size() + 2 * mux.size()) + 2 <= s->max_batch) mux.push_back({c, g});
-            } else if ((int32_t)lin.size() < s->max_batch) {
-                lin.push_back({c, g});
-            }
-        }
+    tfhe_gpu_status st = retire(s, false);
+    if (st != TFHE_GPU_OK) return st;
+    admit(s);
+    if (s->ready.empty() && s->admitted_now.empty()) {
+        // nothing to run: wait for the oldest tick in flight, if any
+        return retire(s, true);
     }
-    const int32_t W = s->width;
-    int32_t* hi = s->h_idx;
-    // linear gates first (no bootstrap): NOT, COPY, CONSTANT
-    if (!lin.empty()) {
-        for (size_t i = 0; i < lin.size(); ++i) {
-            const Gate& G = lin[i].c->gates[lin[i].g];
-            hi[3 * i] = lin[i].c->slot[lin[i].c->ninputs + lin[i].g];
-            hi[3 * i + 1] = G.type == 13 ? -1 : lin[i].c->slot[G.in[0]];
-            hi[3 * i + 2] = G.type == 12 ? 0 : (G.type == 11 ? 1 : (G.in[0] ? 2 : 3));
-        }
-        SCK(s, cudaMemcpyAsync(s->d_lin, hi, sizeof(int32_t) * 3 * lin.size(), cudaMemcpyHostToDevice, st));
-        k_linear<<<grid_for(lin.size() * W), 256, 0, st>>>(s->d_pool, s->d_lin, W, (int)lin.size());
-        SCK(s, cudaGetLastError());
-        SCK(s, cudaStreamSynchronize(st));  // pinned staging is reused below
+    if (s->next_tick - s->next_retire >= kInFlight) {
+        st = retire(s, true);  // frees the staging of tick next_tick - kInFlight
+        if (st != TFHE_GPU_OK) return st;
+        admit(s);
     }
-    // All bootstraps of the tick in one blind-rotation launch.  Items:
-    // [plain gates | MUX first halves AND(a, b) | MUX second halves
-    // ANDNY(a, c)]; the MUX halves are summed with (0, 1/8) before their key
-    // switch (upstream bootsMUX).
-    const int32_t nr = (int32_t)boot.size(), nm = (int32_t)mux.size();
-    const int32_t nb = nr + 2 * nm;
-    if (nb > 0) {
-        int32_t* ha = hi;
-        int32_t* hb = hi + nb;
-        int32_t* hd = hi + 2 * nb;
-        int32_t* hg = hi + 3 * nb;
-        for (int32_t i = 0; i < nr; ++i) {
-            const Gate& G = boot[i].c->gates[boot[i].g];
-            ha[i] = boot[i].c->slot[G.in[0]];
-            hb[i] = boot[i].c->slot[G.in[1]];
-            hg[i] = G.type;
-            hd[i] = boot[i].c->slot[boot[i].c->ninputs + boot[i].g];
-        }
-        for (int32_t j = 0; j < nm; ++j) {
-            const Gate& G = mux[j].c->gates[mux[j].g];
-            const int32_t* sl = mux[j].c->slot.data();
-            ha[nr + j] = sl[G.in[0]];
-            hb[nr + j] = sl[G.in[1]];
-            hg[nr + j] = TFHE_GATE_AND;
-            ha[nr + nm + j] = sl[G.in[0]];
-            hb[nr + nm + j] = sl[G.in[2]];
-            hg[nr + nm + j] = TFHE_GATE_ANDNY;
-            hd[nr + j] = sl[mux[j].c->ninputs + mux[j].g];
-        }
-        SCK(s, cudaMemcpyAsync(s->d_idx, hi, sizeof(int32_t) * 3 * nb, cudaMemcpyHostToDevice, st));
-        SCK(s, cudaMemcpyAsync(s->d_gates, hg, sizeof(int32_t) * nb, cudaMemcpyHostToDevice, st));
-        const int grid = grid_for((size_t)nb * W);
-        k_gather<<<grid, 256, 0, st>>>(s->d_pool, s->d_idx, s->d_a, W, nb);
-        k_gather<<<grid, 256, 0, st>>>(s->d_pool, s->d_idx + nb, s->d_b, W, nb);
-        SCK(s, cudaGetLastError());
-        tfhe_gpu_ctx* ctx = s->ctx;
-        SCK(s, launch_gate_combine(ctx->dp, s->d_gates, 0, s->d_a, s->d_b, s->d_x, nb, st));
-        EpArgs a{};
-        a.err = ctx->d_err;
-        a.x = s->d_x;
-        a.mu = 1 << 29;
-        a.lwe_out = s->d_u;
-        a.gsw = ctx->d_bk[s->form];
-        a.count = nb;
-        SCK(s, launch_external_product(ctx->dp, (Form)s->form, kEpBlindRotate, ctx->tables, a,
-                                       ctx->groups_per_cta[s->form], st));
-        const int32_t EW = s->ext_width;
-        SCK(s, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, s->d_u, s->d_out, nr, st));
-        if (nm) {
-            SCK(s, launch_lwe_add2_const(s->d_u + (size_t)nr * EW, s->d_u + (size_t)(nr + nm) * EW,
-                                         s->d_s, EW, 1 << 29, nm, st));
-            SCK(s, launch_keyswitch(ctx->dp, ctx->d_ks, ctx->ks_row_stride, s->d_s,
-                                    s->d_out + (size_t)nr * W, nm, st));
-        }
-        const int sgrid = grid_for((size_t)(nr + nm) * W);
-        k_scatter<<<sgrid, 256, 0, st>>>(s->d_out, s->d_idx + 2 * nb, s->d_pool, W, nr + nm);
-        SCK(s, cudaGetLastError());
-        SCK(s, cudaStreamSynchronize(st));
-    }
-    const double t1 = now_s();
-    s->busy_s += t1 - t0;
-    // mark done, record latencies
-    auto mark = [&](std::vector<Pick>& picks, bool boots) {
-        for (auto& p : picks) {
-            p.c->done[p.g] = 1;
-            p.c->ready[p.c->ninputs + p.g] = 1;
-            p.c->remaining--;
-            if (boots) record(s->gate_latency, t1 - p.c->ready_at[p.g]);
-        }
-    };
-    mark(lin, false);
-    mark(boot, true);
-    mark(mux, true);
-    s->gates_run += (int64_t)(boot.size() + mux.size() * 2);
-    if (ran) *ran = (int32_t)(boot.size() + mux.size() + lin.size());
-    // retire finished circuits: copy outputs back, free slots
-    for (auto it = s->active.begin(); it != s->active.end();) {
-        Circuit* c = it->second.get();
-        if (c->remaining > 0) {
-            ++it;
-            continue;
-        }
-        c->result.resize((size_t)c->outputs.size() * W);
-        for (size_t o = 0; o < c->outputs.size(); ++o)
-            SCK(s, cudaMemcpyAsync(c->result.data() + o * W,
-                                   s->d_pool + (size_t)c->slot[c->outputs[o]] * W,
-                                   sizeof(int32_t) * W, cudaMemcpyDeviceToHost, st));
-        SCK(s, cudaStreamSynchronize(st));
-        for (int32_t sl : c->slot) s->free_slots.push_back(sl);
-        c->finished = now_s();
-        c->is_done = true;
-        record(s->request_latency, c->finished - c->submitted);
-        s->finished[c->id] = std::move(it->second);
-        it = s->active.erase(it);
-    }
+    Tick& T = s->ticks[s->next_tick % kInFlight];
+    T.index = s->next_tick;
+    schedule(s, T, s->next_tick);
+    int32_t n = (int32_t)(T.boot.size() + T.mux.size());
+    for (auto& level : T.lin) n += (int32_t)level.size();
+    st = enqueue(s, T);
+    if (st != TFHE_GPU_OK) return st;
+    ++s->next_tick;
+    if (ran) *ran = n;
     return TFHE_GPU_OK;
 }
 

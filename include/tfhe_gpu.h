@@ -118,7 +118,12 @@ size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
  *   14 = spread kernel: one ciphertext over 2l groups of 64 threads; per
  *       step each group runs one forward transform, and four of them
  *       multiply all rows for one output part and transform it back (lowest
- *       latency), key rows from L2.
+ *       latency), key rows from L2;
+ *   15 = automatic in fixed summation order: as 0, with the spread kernel
+ *       (two waves) in place of the pair kernel, whose two halves' partial
+ *       products round differently; every launch then sums the key rows in
+ *       the same order, and a ciphertext's result is the same bit for bit
+ *       whatever batch it runs in (the gate server uses it).
  * FP64: 3 (L2) or 4 (ring, in line).  Engine tuning knob, no counterpart in
  * the reference (its kernel is a single HLS work-item). */
 tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,
@@ -298,6 +303,13 @@ tfhe_gpu_status tfhe_gpu_bootsGates_noalloc(tfhe_gpu_ctx* ctx, const int32_t* ga
  * waits.  The context stays usable.  No counterpart in the reference. */
 tfhe_gpu_status tfhe_gpu_selftest_timeout(tfhe_gpu_ctx* ctx, tfhe_gpu_form form, int32_t count);
 
+/* Measured FP32 FMA-pipe peak of `device` in TFLOP/s (and the probe's
+ * duration in ms): independent chains of packed FP32 fused multiply-adds on
+ * every SM, timed with CUDA events, best of 3 after a warm-up.  The
+ * blind-rotation kernels' roofline is quoted against it.  No counterpart in
+ * the reference.  iters = 65536 runs about 20 ms on a GB300. */
+tfhe_gpu_status tfhe_gpu_measure_fp32_peak(int32_t device, int32_t iters, double* tflops, double* ms);
+
 /* ---- CUDA graph of a gate batch; launch-shape autotuner ----------------- */
 /* Capture the whole gate pipeline of one batch (combination, blind rotation
  * and extraction, key switch) over fixed device buffers into a CUDA graph,
@@ -336,7 +348,12 @@ tfhe_gpu_status tfhe_gpu_autotune(tfhe_gpu_ctx* ctx, tfhe_gpu_form form, int32_t
  * {type, in0, in1, in2}: types 0..9 as tfhe_gpu_gate, 10 = MUX (in0 ? in1 :
  * in2), 11 = NOT, 12 = COPY, 13 = CONSTANT (in0 = the bit); wire ids
  * [0, ninputs) are the inputs, ninputs + g the output of gate g, and a
- * gate's inputs must be earlier wires. */
+ * gate's inputs must be earlier wires.  Ticks are pipelined: a gate can be
+ * scheduled once its inputs are scheduled (ticks run in order on the
+ * context's stream), so a step enqueues its tick without waiting for the
+ * one before; at most two ticks are in flight, and a step retires the ticks
+ * it finds complete (outputs of finished circuits copied back inside the
+ * tick, pool slots freed). */
 typedef struct tfhe_gpu_server tfhe_gpu_server;
 tfhe_gpu_status tfhe_gpu_server_create(tfhe_gpu_ctx* ctx, int32_t pool_slots, int32_t max_batch,
                                        tfhe_gpu_form form, tfhe_gpu_server** out);
@@ -347,8 +364,11 @@ tfhe_gpu_status tfhe_gpu_server_submit(tfhe_gpu_server* srv, const int32_t* gate
                                        int32_t ninputs, const int32_t* input_ct,
                                        const int32_t* output_wires, int32_t noutputs,
                                        int64_t* request_id);
-/* One tick: admit, run the ready gates as one batch, retire finished
- * circuits; *ran = gates executed (0 when idle). */
+/* One tick: retire completed ticks, admit, enqueue every schedulable gate
+ * (up to max_batch bootstraps) as one batch; with nothing to schedule it
+ * waits for the oldest tick in flight.  *ran = gates enqueued (0 when there
+ * was nothing to run).  max_batch must be at least 2 (a MUX is two
+ * bootstraps); a circuit needs at least one gate. */
 tfhe_gpu_status tfhe_gpu_server_step(tfhe_gpu_server* srv, int32_t* ran);
 /* Outputs of a finished request (host int32[noutputs][n+1]); *done = 0 while
  * queued or running; latency from submission to completion in seconds. */

@@ -230,7 +230,7 @@ def test_errors_are_status_codes(pkg, keys, torch_cuda, P):
                                          ("split_fp32", 7), ("split_fp32", 8), ("split_fp32", 9),
                                          ("split_fp32", 10), ("split_fp32", 11), ("split_fp32", 12),
                                          ("split_fp32", 13), ("split_fp32", 14),
-                                         ("fp64", 3), ("fp64", 4)])
+                                         ("split_fp32", 15), ("fp64", 3), ("fp64", 4)])
 def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, groups):
     """Each blind-rotation launch shape (L2-direct and shared-ring kernels) on
     a ragged batch: decrypted bits equal the truth and the oracle's, phases
@@ -510,7 +510,7 @@ def test_shapes_agree_bit_for_bit(pkg, keys, torch_cuda, P, inputs):
     try:
         e.upload_bootstrapping_key(keys["bk"], forms=("split_fp32",))
         e.upload_keyswitch_key(keys["ks"])
-        for shape in (1, 2, 4, 5, 6, 7, 8, 9, 10, 14):
+        for shape in (1, 2, 4, 5, 6, 7, 8, 9, 10, 14, 15):
             e.set_groups_per_cta("split_fp32", shape)
             d_out = torch.zeros((count, P.n + 1), dtype=torch.int32, device="cuda")
             e.bootsGates(gates, d_out, dev(torch, ca[:count]), dev(torch, cb[:count]), count, "split_fp32",
@@ -522,3 +522,46 @@ def test_shapes_agree_bit_for_bit(pkg, keys, torch_cuda, P, inputs):
         e.close()
     for shape, out in outs.items():
         assert (out == outs[6]).all(), shape
+
+
+def test_fp32_peak_probe(pkg, torch_cuda):
+    """The FP32 FMA-pipe probe behind the roofline denominator: GB300 has
+    152 SMs x 128 FP32 lanes at up to 2.07 GHz, 80.5 TFLOP/s nominal."""
+    tf, ms = pkg.measure_fp32_peak(0)
+    print("measured FP32 FMA peak: %.1f TFLOP/s (%.2f ms)" % (tf, ms))
+    assert 40.0 <= tf <= 90.0, tf
+
+
+@pytest.mark.parametrize("count", [200, 912 + 200])
+def test_fixed_order_shape_independent_of_batch(pkg, keys, torch_cuda, P, count):
+    """Shape 15 (automatic, fixed summation order) gives every ciphertext the
+    same result bit for bit in a batch of `count` (a 2-per-SM remainder,
+    which shape 0 runs on the pair kernel) and in a batch of 37 (spread
+    kernel)."""
+    torch = torch_cuda
+    rng = np.random.default_rng(231 + count)
+    a = rng.integers(0, 2, count)
+    b = rng.integers(0, 2, count)
+    pkg.set_seed([231 + count])
+    ca = pkg.encrypt_bits(P, a, keys["lwe"])
+    cb = pkg.encrypt_bits(P, b, keys["lwe"])
+    gates = (np.arange(count, dtype=np.int32) * 3) % 10
+    e = pkg.Engine(pkg.default_params())
+    try:
+        e.upload_bootstrapping_key(keys["bk"], forms=("split_fp32",))
+        e.upload_keyswitch_key(keys["ks"])
+        e.set_groups_per_cta("split_fp32", 15)
+        outs = []
+        for lo, hi in ((0, count), (count - 37, count)):
+            d_out = torch.zeros((hi - lo, P.n + 1), dtype=torch.int32, device="cuda")
+            e.bootsGates(dev(torch, gates[lo:hi]), d_out, dev(torch, ca[lo:hi]), dev(torch, cb[lo:hi]), hi - lo,
+                         "split_fp32", stream=cur(torch))
+            torch.cuda.synchronize()
+            e.synchronize()
+            outs.append(host(d_out))
+    finally:
+        e.close()
+    assert (outs[0][count - 37:] == outs[1]).all()
+    names = sorted(pyoracle.GATES, key=lambda g: pyoracle.GATES[g])
+    truth = np.array([pyoracle.GATE_FN[names[g]](x, y) for g, x, y in zip(gates, a, b)])
+    assert (pkg.decrypt_bits(P, outs[0], keys["lwe"]) == truth).all()

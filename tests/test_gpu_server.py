@@ -153,3 +153,31 @@ def test_bad_circuits_are_refused(pkg, engine, circuits):
             srv.submit(big, 2, ct, [2])                   # more wires than slots
     finally:
         srv.close()
+
+
+def test_burst_of_circuits_pipelined(pkg, engine, keys, circuits):
+    """A burst far above one tick's capacity: 180 circuits submitted at once
+    through a server with small batches, so ticks are full, run back to back
+    in the pipeline (two in flight) and finish circuits out of submission
+    order.  Every request decrypts to its plaintext result, the pool is
+    whole again afterwards, and the probe circuit's ciphertexts equal those
+    of the same circuit run alone."""
+    P = pkg.default_params()
+    rng = np.random.default_rng(84)
+    pkg.set_seed([84])
+    jobs, truth = [], []
+    for i in range(180):
+        g, ni, outs, bits = _operands(rng, circuits, ("adder", "cmp", "mux")[i % 3])
+        jobs.append((g, ni, pkg.encrypt_bits(P, bits, keys["lwe"]), outs))
+        truth.append(circuits.evaluate(g, bits, outs))
+    srv = pkg.Server(engine, pool_slots=1 << 16, max_batch=600)
+    try:
+        outs = _run(srv, jobs)
+        for o, t in zip(outs, truth):
+            assert (pkg.decrypt_bits(P, o, keys["lwe"]) == t).all()
+        st = srv.stats()
+        assert st["free_slots"] == 1 << 16 and st["active"] == 0
+        alone = _run(srv, [jobs[7]])[0]
+        assert (alone == outs[7]).all()
+    finally:
+        srv.close()
