@@ -23,9 +23,13 @@ seed 0, input bits from seed 4.  Synthetic data: no dataset is involved.
 restatement; the upstream library the reference links is not available) and
 prints the same line with "impl": "reference".
 
-Multi-GPU (torchrun): each rank runs an independent replica of the step on
-its own GPU (gate bootstraps of a layer are independent); value = all ranks'
-bootstraps / max rank time; "scaling": "weak".
+Multi-GPU (torchrun): the layer's gate list is split into contiguous,
+balanced shards, one per rank; each rank bootstraps its shard on its own GPU
+with its own copy of the cloud key (the gates of a layer are independent),
+and the output ciphertexts are gathered to rank 0 in layer order on the host
+(a gloo group) -- the only exchange between layers.  value = the whole
+layer's bootstraps / max rank time; "scaling": "strong".  --replicas runs
+the whole layer on every rank instead ("scaling": "weak").
 """
 import argparse
 import json
@@ -81,6 +85,8 @@ def parse():
     ap.add_argument("--rate", type=float, default=8.0, help="requests/s per client (serve)")
     ap.add_argument("--groups", type=int, default=0,
                     help="ciphertexts per CTA of the split-FP32 blind rotation (0 = engine default)")
+    ap.add_argument("--replicas", action="store_true",
+                    help="N > 1: every rank runs the whole layer (weak scaling) instead of a shard of it")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64 / single-gate / CPU side measurements")
     return ap.parse_args()
@@ -110,14 +116,46 @@ def job_throughput(units_per_rank, world, max_ms):
     return world * units_per_rank / (max_ms / 1000.0)
 
 
-def layer_config(batch):
+def layer_config(batch, world=1, replicas=False):
     """The workload's `config`, identical in both arms (the reference arm
     times a bounded sample of this workload and says so in its
     cpu_baseline.sample)."""
+    if world <= 1:
+        par = "one GPU"
+    elif replicas:
+        par = "replicas: the whole layer on each of %d GPUs" % world
+    else:
+        par = "layer split: contiguous shards over %d GPUs, host-side gather to rank 0" % world
     return {"workload": "batched circuit layer: %d independent gate bootstraps, mixed NAND/AND/XOR/OR "
                         "(seed 4), default 110-bit set (n=630, N=1024, k=1, l=3, Bgbit=7, t=8, basebit=2), "
                         "one cloud key (seed 0)" % batch,
-            "batch": batch, "l2": "flushed (256 MB write) between timed steps", "parallelism": "replicas"}
+            "batch": batch, "l2": "flushed (256 MB write) between timed steps", "parallelism": par}
+
+
+def layer_shards(count, world):
+    """Contiguous, balanced shards [lo, hi) of a layer's `count` gates over
+    `world` ranks (sizes differ by at most one, in rank order)."""
+    return [(r * count // world, (r + 1) * count // world) for r in range(world)]
+
+
+def gather_layer(shard_out, count, world, rank, group=None):
+    """Host-side gather of the ranks' output shards (int32 [hi - lo, n + 1]
+    each) to rank 0 in layer order: the whole layer's outputs on rank 0,
+    None on the other ranks.  Shards are padded to the largest size for the
+    collective."""
+    if world <= 1:
+        return shard_out
+    import torch
+    import torch.distributed as dist
+    shards = layer_shards(count, world)
+    rows = max(hi - lo for lo, hi in shards)
+    buf = torch.zeros((rows, shard_out.shape[1]), dtype=torch.int32)
+    buf[:len(shard_out)] = torch.from_numpy(np.ascontiguousarray(shard_out, np.int32))
+    parts = [torch.zeros_like(buf) for _ in range(world)] if rank == 0 else None
+    dist.gather(buf, parts, dst=0, group=group)
+    if rank != 0:
+        return None
+    return np.concatenate([parts[r][:hi - lo].numpy() for r, (lo, hi) in enumerate(shards)])
 
 
 def make_inputs(pkg, P, lwe_key, batch, seed=4):
@@ -257,7 +295,7 @@ def run_reference(args, world, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": layer_config(args.batch),
+        "config": layer_config(args.batch, world, getattr(args, "replicas", False)),
         "cpu_baseline": {"value": value, "unit": "bootstraps/s", "cores": threads, "kind": "port",
                          "sample": "each step a bounded sample of %d gates of the %d-gate layer (same gate "
                                    "mix, keys and inputs), %d steps, FP64 2N-point transform restatement "
@@ -659,9 +697,11 @@ def main():
     import __graft_entry__ as ge
 
     torch.cuda.set_device(local)
+    host_group = None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
+        host_group = dist.new_group(backend="gloo")  # the host-side ciphertext gather
     ge.build()
     pkg = ge.load_package()
     P = pkg.default_params()
@@ -670,7 +710,10 @@ def main():
     eng = pkg.Engine(P, device=local)
     eng.upload_bootstrapping_key(bk, forms=("fp64", "split_fp32"))
     eng.upload_keyswitch_key(ks)
-    batch = args.batch
+    split = world > 1 and not args.replicas
+    lo, hi = layer_shards(args.batch, world)[rank] if split else (0, args.batch)
+    batch = hi - lo  # this rank's gates
+    layer_units = args.batch if split else world * args.batch  # bootstraps of the job per step
     tuned = None
     if args.groups:
         eng.set_groups_per_cta(args.form, args.groups)
@@ -678,7 +721,8 @@ def main():
         # project autotuner: time every launch shape on this batch size
         shape, br_ms = eng.autotune(args.form, batch)
         tuned = {"shape": shape, "blind_rotate_ms": br_ms}
-    a, b, gates, ca, cb = make_inputs(pkg, P, lwe, batch)
+    a_all, b_all, gates_all, ca_all, cb_all = make_inputs(pkg, P, lwe, args.batch)
+    a, b, gates, ca, cb = (x[lo:hi] for x in (a_all, b_all, gates_all, ca_all, cb_all))
     dev = torch.device("cuda", local)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
     # a non-default stream: the engine maps a NULL stream to its own stream,
@@ -726,15 +770,20 @@ def main():
         ms = timed(args.form, args.steps)
     torch.cuda.synchronize()
     total_ms = max_over_ranks(sum(ms), world, dev)
-    value = job_throughput(batch * args.steps, world, total_ms)
+    value = layer_units * args.steps / (total_ms / 1000.0)
     truth = {0: lambda x, y: 1 - (x & y), 1: lambda x, y: x & y, 2: lambda x, y: x | y,
              3: lambda x, y: x ^ y}
     d_out.zero_()
     step(args.form)
     torch.cuda.synchronize()
     out = d_out.cpu().numpy()
-    ok = bool((pkg.decrypt_bits(P, out, lwe)
-               == np.array([truth[int(g)](x, y) for g, x, y in zip(gates, a, b)])).all())
+    if split:
+        out = gather_layer(out, args.batch, world, rank, host_group)
+    ok = None
+    if out is not None:  # rank 0 checks the whole layer it holds
+        ga, aa, ba = (gates_all, a_all, b_all) if split else (gates, a, b)
+        ok = bool((pkg.decrypt_bits(P, out, lwe)
+                   == np.array([truth[int(g)](x, y) for g, x, y in zip(ga, aa, ba)])).all())
 
     # e2e through the host-buffer entry point (pinned host buffers)
     h_ca = torch.from_numpy(ca).pin_memory()
@@ -752,10 +801,12 @@ def main():
             pkg.ctypes.cast(h_cb.data_ptr(), pkg.I32P), batch, pkg.FORMS[args.form])
         if st:
             raise RuntimeError("bootsGates_host failed: %d" % st)
+        if split:  # the between-layer exchange: outputs to rank 0 in layer order
+            gather_layer(h_out.numpy(), args.batch, world, rank, host_group)
         if s >= args.warmup:
             e2e_ms.append(1000 * (time.perf_counter() - t0))
     e2e_total = max_over_ranks(sum(e2e_ms), world, dev)
-    e2e_value = job_throughput(batch * args.steps, world, e2e_total)
+    e2e_value = layer_units * args.steps / (e2e_total / 1000.0)
     lwe_bytes = batch * (P.n + 1) * 4
 
     # dominant kernels alone: blind rotation + extraction on resident inputs
@@ -861,11 +912,12 @@ def main():
         line = {
             "metric": "gate bootstraps/sec", "value": value, "unit": "bootstraps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "strong" if split else "weak",
             "vs_baseline": None, "dtype": "f32" if args.form == "split_fp32" else "f64",
             "data": "synthetic",
-            "config": layer_config(batch),
-            "engine": {"form": args.form, "split_bits": eng.params.split_bits,
+            "config": layer_config(args.batch, world, args.replicas),
+            "engine": {"form": args.form, "split_bits": eng.params.split_bits, "gates_per_rank": batch,
                        "groups_per_cta": eng.get_groups_per_cta(args.form),
                        "autotune": tuned, "cuda_graph": graph is not None},
             "latency_ms": {"p50": p50, "p99": p99,

@@ -1,8 +1,10 @@
-"""The multi-GPU path of bench.py is replicas only: each rank runs the whole
-gate layer on its own GPU, and the only cross-rank step is the maximum of
-the ranks' times (plus a barrier).  Covered here with world size 2 on the
-gloo backend (CPU): the aggregation, the job throughput, and the reference
-arm printing on rank 0 only."""
+"""The multi-GPU path of bench.py: the layer's gate list is split into
+contiguous shards, one per rank, each rank bootstraps its shard on its own
+GPU, and the output ciphertexts are gathered to rank 0 on the host (the
+between-layer exchange); the job's time is the slowest rank's.  (--replicas:
+the whole layer on every rank.)  Covered here with world size 2 on the gloo
+backend (CPU): the partition, the gather's order, the aggregation, the job
+throughput, and the reference arm printing on rank 0 only."""
 import multiprocessing as mp
 import os
 import socket
@@ -60,6 +62,66 @@ def test_replicas_aggregate_with_gloo():
         assert (w, r, loc) == (world, rank, rank)
         assert mx == 120.0  # the slowest rank's time
         assert abs(value - 2 * 4096 * 10 / 0.120) < 1e-6
+
+
+def _gather_main(rank, world, port, count, q):
+    try:
+        os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port), "RANK": str(rank),
+                           "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank)})
+        sys.path.insert(0, ROOT)
+        import numpy as np
+        import torch.distributed as dist
+        import bench
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+        lo, hi = bench.layer_shards(count, world)[rank]
+        # this rank's "outputs": row g holds (g, rank, g * 7) -- the gate
+        # index it computed, the rank that computed it, a payload
+        rows = np.array([[g, rank, g * 7] for g in range(lo, hi)], np.int32).reshape(-1, 3)
+        full = bench.gather_layer(rows, count, world, rank)
+        dist.destroy_process_group()
+        q.put((rank, None if full is None else full.tolist()))
+    except Exception as e:  # reported to the parent
+        q.put((rank, "error", repr(e)))
+
+
+@pytest.mark.parametrize("count", [4096, 37, 1])
+def test_layer_split_and_gather_with_gloo(count):
+    """Each rank bootstraps a contiguous shard of the layer; rank 0 receives
+    every gate's output exactly once, in layer order (shards of unequal size
+    included; a 1-gate layer leaves rank 1 an empty shard)."""
+    pytest.importorskip("torch")
+    world = 2
+    port = _free_port()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_gather_main, args=(r, world, port, count, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = dict((r[0], r[1:]) for r in (q.get(timeout=120) for _ in range(world)))
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res[0][0] != "error" and res[1][0] != "error", res
+    assert res[1][0] is None
+    full = res[0][0]
+    assert [row[0] for row in full] == list(range(count))
+    assert [row[2] for row in full] == [7 * g for g in range(count)]
+    sys.path.insert(0, ROOT)
+    import bench
+    shards = bench.layer_shards(count, world)
+    assert [row[1] for row in full] == [r for r, (lo, hi) in enumerate(shards) for _ in range(lo, hi)]
+
+
+def test_layer_shards_cover_the_layer():
+    sys.path.insert(0, ROOT)
+    import bench
+    for count in (1, 7, 4096, 4097):
+        for world in (1, 2, 3, 8):
+            sh = bench.layer_shards(count, world)
+            assert sh[0][0] == 0 and sh[-1][1] == count
+            assert all(sh[i][1] == sh[i + 1][0] for i in range(world - 1))
+            sizes = [hi - lo for lo, hi in sh]
+            assert max(sizes) - min(sizes) <= 1
 
 
 def test_single_rank_is_identity():
