@@ -851,8 +851,8 @@ def main():
             torch.cuda.synchronize()
             one_ms.append(e0.elapsed_time(e1))
         one = statistics.median(one_ms[1:])
-        # a single gate on the automatic shape (pair kernel), whatever shape
-        # the autotuner kept for the full batch
+        # a single gate on the automatic shape (the spread kernel over a
+        # two-SM cluster), whatever shape the autotuner kept for the batch
         saved_shape = eng.get_groups_per_cta("split_fp32")
         eng.set_groups_per_cta("split_fp32", 0)
         one32 = []
@@ -864,8 +864,28 @@ def main():
             e1.record(stream)
             torch.cuda.synchronize()
             one32.append(e0.elapsed_time(e1))
+        # its blind rotation alone: the whole key streamed once for one gate
+        u1 = torch.empty((1, P.k * P.N + 1), dtype=torch.int32, device=dev)
+        br1 = []
+        for s in range(4):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.tfhe_bootstrap_woKS_FFT(u1, d_ca[:1], 2 ** 29, 1, "split_fp32", stream=sp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            br1.append(e0.elapsed_time(e1))
+        br1_ms = statistics.median(br1[1:])
         eng.set_groups_per_cta("split_fp32", saved_shape)
         extras["split_fp32_single_gate_ms"] = statistics.median(one32[1:])
+        key_bytes = 61931520.0
+        extras["single_gate_key_stream"] = {
+            "blind_rotate_ms": br1_ms, "key_bytes": key_bytes,
+            "achieved_gbs": key_bytes / (br1_ms / 1000.0) / 1e9,
+            "hbm_floor_us": key_bytes / (_measured_peak("hbm_gbs") * 1e9) * 1e6,
+            "hbm_frac": key_bytes / (br1_ms / 1000.0) / 1e9 / _measured_peak("hbm_gbs"),
+            "note": "batch 1: the 61.9 MB key streamed once through a chain of n dependent steps; "
+                    "latency-bound, not bandwidth-bound"}
         extras["fp64_single_gate_ms"] = one
         extras["fp64_single_gate_bootstraps_per_s"] = 1000.0 / one
         extras["speedup_vs_fp64_single_gate"] = value / world / (1000.0 / one)
@@ -1016,7 +1036,8 @@ def blind_rotate_kernels(form, shape, batch, l=3):
     pairs = "k_blind_rotate_ring<float,2,6,%d,4,inline,nb2>" % l
     pair = "k_blind_rotate_pair<float,2,%d,%d,4>"
     spread = "k_blind_rotate_spread<%d>" % l
-    if shape == 0:
+    spread2 = "k_blind_rotate_spread2<%d>" % l
+    if shape in (0, 15):
         wave = 6 * SMS
         full, rest = (batch // wave) * wave, batch - (batch // wave) * wave
         if rest == 0 or rest > 4 * SMS:
@@ -1024,11 +1045,15 @@ def blind_rotate_kernels(form, shape, batch, l=3):
         names = [pairs + " x %d" % full] if full else []
         if rest > 2 * SMS:
             return names + [batched + " x %d" % rest]
-        if rest > SMS:
+        if rest > SMS and shape == 0:
             return names + [pair % (2, l) + " x %d" % rest]
-        return names + [spread + " x %d" % rest]
+        if rest > SMS // 2:
+            return names + [spread + " x %d" % rest]
+        return names + [spread2 + " x %d" % rest]
     if shape == 14:
         return [spread]
+    if shape == 16:
+        return [spread2]
     if shape == 9:
         return [batched]
     if shape == 10:

@@ -500,9 +500,9 @@ class Engine:
         split_fp32: 0 automatic; 1, 2, 4 L2-direct; 5-8 shared key ring, one
         transform at a time; 9 ring, 4 per CTA, a step's transforms
         together; 10 ring, 6 per CTA, two at a time; 11-13 pair kernel;
-        14 spread kernel (lowest latency); 15 automatic in fixed summation
-        order (no pair kernel: results independent of the batch).  fp64: 3
-        or 4."""
+        14 spread kernel; 15 automatic in fixed summation order (no pair
+        kernel: results independent of the batch); 16 spread kernel over a
+        two-SM cluster (lowest latency).  fp64: 3 or 4."""
         self._check(self.lib.tfhe_gpu_set_groups_per_cta(self.ctx, self._form(form), int(groups)),
                     "set_groups_per_cta")
 

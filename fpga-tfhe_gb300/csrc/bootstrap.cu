@@ -21,6 +21,7 @@
 //   TorusPolynomial_fft          .../TorusPolynomial_fft.cpp:4-43
 //   modulus switch / test vector kernel/src/tfhe_bootstrap_woKS_FFT/tfhe_bootstrap_woKS_FFT.cpp:3-10,57-66
 //   X^{2N-b} rotation            kernel/src/tfhe_blindRotateAndExtract/mulByXaiOrCopy.cpp:25-41
+#include <cooperative_groups.h>
 #include <math.h>
 
 #include "async_copy.cuh"
@@ -902,6 +903,18 @@ __global__ void __launch_bounds__(128 * L, 1) k_blind_rotate_spread(KParams kp, 
         if (i + 1 < n && threadIdx.x < kRows)  // the next step's rows into L2
             bulk_prefetch_l2(step_keys + step_elems + (size_t)threadIdx.x * kRowElems,
                              kRowElems * sizeof(cpx<float>));
+        // the owners' key loads go out first: their L2 latency overlaps the
+        // rotation, the digits and the forward transform
+        float4 kk[kRows][4];
+        if (owner) {
+#pragma unroll
+            for (int p = 0; p < kRows; ++p) {
+                const float4* g4 =
+                    reinterpret_cast<const float4*>(step_keys + (size_t)p * kRowElems + (oj * 2 + opt) * kHalf);
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) kk[p][qq] = __ldg(g4 + qq * 64 + t);
+            }
+        }
         cpx<float> v[8];
         {
             const int32_t* src = acc + jp * kN;
@@ -917,16 +930,6 @@ __global__ void __launch_bounds__(128 * L, 1) k_blind_rotate_spread(KParams kp, 
         fft512_forward_tw(v, sc, tw, ix, t, bar_id);
 #pragma unroll
         for (int q = 0; q < 8; ++q) dsh[(g * 8 + q) * 64 + t] = v[q];
-        float4 kk[kRows][4];
-        if (owner) {
-#pragma unroll
-            for (int p = 0; p < kRows; ++p) {
-                const float4* g4 =
-                    reinterpret_cast<const float4*>(step_keys + (size_t)p * kRowElems + (oj * 2 + opt) * kHalf);
-#pragma unroll
-                for (int qq = 0; qq < 4; ++qq) kk[p][qq] = __ldg(g4 + qq * 64 + t);
-            }
-        }
         __syncthreads();  // every D written, every read of acc done
         if (owner) {
             cpx<float> o[8];
@@ -965,6 +968,167 @@ __global__ void __launch_bounds__(128 * L, 1) k_blind_rotate_spread(KParams kp, 
             dst[i] = i == 0 ? acc[0] : (int32_t)(0u - (uint32_t)acc[kN - i]);
         if (threadIdx.x == 0) dst[kN] = acc[kN];
     }
+}
+
+// ----------------------------------------------------------------------
+// Blind rotation with one ciphertext over a cluster of two CTAs (two SMs).
+//
+// The spread kernel's work split across two SMs: CTA r of the cluster holds
+// accumulator polynomial r, runs the l forward transforms of polynomial r
+// (one per group) and owns output polynomial r (groups 0 and 1: the high and
+// the low key part).  Each group writes its transformed digits D_(r,lev) to
+// its own shared memory and pushes them into the peer CTA's (distributed
+// shared memory); after one cluster barrier the owners multiply all 2l rows
+// -- l local, l from the peer -- in row order with their part of each key
+// row, transform back, round and add into the local accumulator with
+// integer atomics.  The accumulator never crosses SMs, only 4 KB of digits
+// per group and step do.  The pushes alternate between two buffers, so the
+// one cluster barrier per step also orders a push after the peer's reads of
+// the buffer two steps back.  Each SM carries half the spread kernel's
+// shared-memory traffic and transforms; the products are summed in the same
+// order as every other shape, so the ciphertexts are bit-identical to the
+// spread kernel's.  Split-FP32 only, 1 CTA per SM (the shared-memory request
+// is padded so that the two CTAs take two SMs).
+// ----------------------------------------------------------------------
+template <int L>
+struct Spread2Plan {
+    static constexpr size_t tables = kHotSize * sizeof(cpx<float>);
+    static constexpr size_t acc_off = tables;                                     // own polynomial
+    static constexpr size_t dloc_off = acc_off + kN * sizeof(int32_t);           // [lev][q][t]
+    static constexpr size_t drem_off = dloc_off + L * kHalf * sizeof(cpx<float>);  // [buf][lev][q][t]
+    static constexpr size_t scratch_off = drem_off + 2 * L * kHalf * sizeof(cpx<float>);
+    static constexpr size_t scratch = 2 * kScratchStride * sizeof(cpx<float>);
+    static constexpr size_t total = scratch_off + L * scratch;
+    static constexpr size_t request = total > 120 * 1024 ? total : 120 * 1024;  // one CTA per SM
+};
+
+template <int L>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 * L, 1)
+    k_blind_rotate_spread2(KParams kp, Tables T, EpArgs a) {
+    static_assert(L >= 2, "two owner groups per CTA");
+    namespace cg = cooperative_groups;
+    using Plan = Spread2Plan<L>;
+    constexpr int kRows = 2 * L;
+    constexpr int kRowElems = 2 * 2 * kHalf;  // complex values per key row
+    extern __shared__ __align__(128) char smem[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int r = (int)cluster.block_rank();  // this CTA's polynomial
+    cpx<float>* tables = reinterpret_cast<cpx<float>*>(smem);
+    int32_t* acc = reinterpret_cast<int32_t*>(smem + Plan::acc_off);
+    cpx<float>* dloc = reinterpret_cast<cpx<float>*>(smem + Plan::dloc_off);
+    cpx<float>* drem = reinterpret_cast<cpx<float>*>(smem + Plan::drem_off);
+    cpx<float>* drem_peer = cluster.map_shared_rank(drem, (unsigned)(r ^ 1));
+    const int c = blockIdx.x >> 1;
+    const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
+    const int lev = g;
+    const bool owner = g < 2;
+    const int opt = g & 1;
+    const int n = kp.n;
+    load_hot_tables<float>(tables, T);
+    if (a.acc_in) {
+        const int32_t* src = a.acc_in + (size_t)c * 2 * kN + (size_t)r * kN;
+        for (int i = threadIdx.x; i < kN; i += blockDim.x) acc[i] = src[i];
+    } else {
+        const int32_t* xs = a.x + (size_t)c * (n + 1);
+        const int barb = mod_switch_2n(xs[n]);
+        for (int i = threadIdx.x; i < kN; i += blockDim.x) acc[i] = r == 0 ? 0 : test_vector_coef(a, c, barb, i);
+    }
+    __syncthreads();
+
+    const FftTwiddles<float> tw = hot_twiddles<float>(tables);
+    const FftIdx ix = make_fft_idx(t);
+    const FftScratch<float> sc = scratch_at<float>(smem + Plan::scratch_off + (size_t)g * Plan::scratch);
+    const int bar_id = 1 + g;
+    const int halfBg = 1 << (kp.Bgbit - 1);
+    const uint32_t mask = (1u << kp.Bgbit) - 1;
+    const int decal = 32 - (lev + 1) * kp.Bgbit;
+    const cpx<float>* gsw = reinterpret_cast<const cpx<float>*>(a.gsw);
+    const size_t step_elems = (size_t)kRows * kRowElems;
+    const int32_t* bara = a.bara ? a.bara + (size_t)c * n : nullptr;
+    const int32_t* xs = a.x ? a.x + (size_t)c * (n + 1) : nullptr;
+    int a_next = bara ? bara[0] : mod_switch_2n(xs[0]);
+    if (threadIdx.x < kRows && (threadIdx.x & 1) == r)
+        bulk_prefetch_l2(gsw + (size_t)threadIdx.x * kRowElems, kRowElems * sizeof(cpx<float>));
+    int buf = 0;
+#pragma unroll 1
+    for (int i = 0; i < n; ++i) {
+        const int ai = a_next;
+        if (i + 1 < n) a_next = bara ? bara[i + 1] : mod_switch_2n(xs[i + 1]);
+        if (ai == 0) continue;  // tfhe_blindRotate_FFT.cpp:114 (uniform over the cluster)
+        const cpx<float>* step_keys = gsw + (size_t)i * step_elems;
+        if (i + 1 < n && threadIdx.x < kRows && (threadIdx.x & 1) == r)  // next step's rows into L2
+            bulk_prefetch_l2(step_keys + step_elems + (size_t)threadIdx.x * kRowElems,
+                             kRowElems * sizeof(cpx<float>));
+        float4 kk[kRows][4];
+        if (owner) {  // part (r, opt) of every row, issued before the transform
+#pragma unroll
+            for (int p = 0; p < kRows; ++p) {
+                const float4* g4 =
+                    reinterpret_cast<const float4*>(step_keys + (size_t)p * kRowElems + (r * 2 + opt) * kHalf);
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) kk[p][qq] = __ldg(g4 + qq * 64 + t);
+            }
+        }
+        cpx<float> v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int x0 = t + 64 * q;
+            const uint32_t u0 = (uint32_t)rot_coef(acc, x0, ai) - (uint32_t)acc[x0] + kp.offset;
+            const uint32_t u1 = (uint32_t)rot_coef(acc, x0 + kHalf, ai) - (uint32_t)acc[x0 + kHalf] + kp.offset;
+            v[q] = digit_pair<float>(u0, u1, decal, mask, halfBg);
+        }
+        fft512_forward_tw(v, sc, tw, ix, t, bar_id);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            dloc[(lev * 8 + q) * 64 + t] = v[q];
+            drem_peer[((buf * L + lev) * 8 + q) * 64 + t] = v[q];
+        }
+        cluster.sync();  // every D of both polynomials in place; every read of acc done
+        if (owner) {
+            cpx<float> o[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) o[q] = {0.f, 0.f};
+#pragma unroll
+            for (int p = 0; p < kRows; ++p) {
+                const int jp = p / L, lv = p - jp * L;
+                const cpx<float>* D = jp == r ? dloc + lv * kHalf : drem + (buf * L + lv) * kHalf;
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) {
+                    const cpx<float> d0 = D[(2 * qq) * 64 + t];
+                    const cpx<float> d1 = D[(2 * qq + 1) * 64 + t];
+                    o[2 * qq] = cmac(o[2 * qq], d0, cpx<float>{kk[p][qq].x, kk[p][qq].y});
+                    o[2 * qq + 1] = cmac(o[2 * qq + 1], d1, cpx<float>{kk[p][qq].z, kk[p][qq].w});
+                }
+            }
+            fft512_inverse_tw(o, sc, tw, ix, t, bar_id);
+            uint32_t c0[8] = {}, c1[8] = {};  // the low part adds into them
+            round_part<float, 2>(o, opt, kp.split, c0, c1);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int x0 = t + 64 * q;
+                atomicAdd(reinterpret_cast<unsigned*>(acc + x0), c0[q]);
+                atomicAdd(reinterpret_cast<unsigned*>(acc + x0 + kHalf), c1[q]);
+            }
+        }
+        buf ^= 1;
+        __syncthreads();  // the accumulator is updated before the next step reads it
+    }
+    if (a.acc_out) {
+        int32_t* dst = a.acc_out + (size_t)c * 2 * kN + (size_t)r * kN;
+        for (int i = threadIdx.x; i < kN; i += blockDim.x) dst[i] = acc[i];
+    }
+    if (a.lwe_out) {
+        // tLweExtractLweSample: a'_0 = a_0, a'_j = -a_{N-j} (polynomial 0),
+        // b' = b_0 (polynomial 1)
+        int32_t* dst = a.lwe_out + (size_t)c * (kN + 1);
+        if (r == 0) {
+            for (int i = threadIdx.x; i < kN; i += blockDim.x)
+                dst[i] = i == 0 ? acc[0] : (int32_t)(0u - (uint32_t)acc[kN - i]);
+        } else if (threadIdx.x == 0) {
+            dst[kN] = acc[0];
+        }
+    }
+    cluster.sync();  // no CTA leaves while its peer could still address its shared memory
 }
 
 // ----------------------------------------------------------------------
@@ -1550,6 +1714,18 @@ cudaError_t launch_spread(const DevParams& P, const Tables& T, const EpArgs& a, 
     return cudaGetLastError();
 }
 
+template <int L>
+cudaError_t launch_spread2(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
+    if (a.count <= 0) return cudaSuccess;
+    const KParams kp = make_kparams(P);
+    using Plan = Spread2Plan<L>;
+    auto kern = k_blind_rotate_spread2<L>;
+    cudaError_t e = set_smem(kern, Plan::request);
+    if (e != cudaSuccess) return e;
+    kern<<<2 * a.count, 64 * L, Plan::request, st>>>(kp, T, a);
+    return cudaGetLastError();
+}
+
 // split-FP32 pair kernel with `per_cta` (1..3) ciphertexts per CTA
 template <int L>
 cudaError_t launch_pair_fp32(const DevParams& P, const Tables& T, const EpArgs& a, int per_cta,
@@ -1577,11 +1753,13 @@ cudaError_t launch_ring_pairs(const DevParams& P, const Tables& T, const EpArgs&
 // Measured per launch (default set): a wave of 6 per SM on
 // launch_ring_pairs 6.6 ms (138K gates/s), of 4 per SM on
 // launch_ring_batched 4.6 ms (132K/s), whatever the fill of the wave; the
-// spread kernel 1.9 ms at 1 per SM (3.8 ms for two waves); the pair kernel
-// 2.6 ms at 1 per SM, 3.3 ms at 2, 5.1 ms at 3.  So: whole waves of 6 per
-// SM; a remainder of at most 1 per SM on the spread kernel, of 2 per SM on
-// the pair kernel, of at most 4 per SM as one launch_ring_batched wave, else
-// one more 6-per-SM wave.
+// spread kernel over a two-SM cluster 1.35 ms for up to one per two SMs;
+// the spread kernel 1.85 ms at 1 per SM (3.7 ms for two waves); the pair
+// kernel 2.6 ms at 1 per SM, 3.3 ms at 2, 5.1 ms at 3.  So: whole waves of
+// 6 per SM; a remainder of at most one per two SMs on the cluster spread
+// kernel, of at most 1 per SM on the spread kernel, of 2 per SM on the pair
+// kernel, of at most 4 per SM as one launch_ring_batched wave, else one
+// more 6-per-SM wave.
 //
 // fixed_order (shape 15): the pair kernel, which adds its two halves' partial
 // products and so may round differently, is replaced by the spread kernel
@@ -1602,7 +1780,8 @@ cudaError_t launch_auto_fp32(const DevParams& P, const Tables& T, const EpArgs& 
     const EpArgs tail = slice_blind_rotate(P, a, full, rest);
     if (rest > 2 * kSmCount) return launch_ring_batched<L>(P, T, tail, st);
     if (rest > kSmCount && !fixed_order) return launch_pair_fp32<L>(P, T, tail, 2, st);
-    return launch_spread<L>(P, T, tail, st);
+    if (rest > kSmCount / 2) return launch_spread<L>(P, T, tail, st);
+    return launch_spread2<L>(P, T, tail, st);
 }
 
 // FP64: ~250 registers per thread and 2 x L exchange buffers of 9 KB per
@@ -1625,12 +1804,14 @@ cudaError_t launch_ep_l(const DevParams& P, Form f, EpMode mode, const Tables& T
     default:
         if (groups == 0) return launch_auto_fp32<L>(P, T, a, st);
         if (groups == 15) return launch_auto_fp32<L>(P, T, a, st, true);
+        if (groups == 16) return launch_spread2<L>(P, T, a, st);
         // 1, 2, 4: L2-direct key reads; 5: shared ring fed by a producer
         // warp; 6, 7, 8: shared ring fed in line by one consumer thread;
         // 9: shared ring, 4 per CTA, a step's l forward transforms run
         // together; 10: shared ring, 6 per CTA, transforms two at a time;
         // 11, 12, 13: pair kernel with 1, 2, 3 ciphertexts per CTA;
-        // 15: the automatic shape in fixed summation order (no pair kernel)
+        // 15: the automatic shape in fixed summation order (no pair kernel);
+        // 16: spread over a cluster of two CTAs
         if (groups >= 11 && groups <= 13) return launch_pair_fp32<L>(P, T, a, groups - 10, st);
         if (groups == 9) return launch_ring_batched<L>(P, T, a, st);
         if (groups == 10) return launch_ring_pairs<L>(P, T, a, st);

@@ -322,7 +322,7 @@ tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form for
                                             int32_t groups) {
     if (!ctx || !form_ok(form)) return TFHE_GPU_BAD_PARAM;
     const bool ok = form == TFHE_GPU_FP64 ? (groups == 3 || groups == 4)
-                                          : ((groups >= 0 && groups <= 15 && groups != 3));
+                                          : ((groups >= 0 && groups <= 16 && groups != 3));
     if (!ok) return fail(ctx, TFHE_GPU_BAD_PARAM, "unsupported groups per CTA for this form");
     ctx->groups_per_cta[form] = groups;
     return TFHE_GPU_OK;

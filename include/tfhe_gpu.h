@@ -102,9 +102,9 @@ size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
 
 /* Launch shape of the blind-rotation kernel of `form`.  split-FP32:
  *   0 = automatic: whole waves of 6 ciphertexts per SM on shape 10; a
- *       remainder of at most 1 per SM on shape 14, of 2 per SM on the pair
- *       kernel, of at most 4 per SM as one shape-9 wave, else one more
- *       shape-10 wave;
+ *       remainder of at most one per two SMs on shape 16, of at most 1 per
+ *       SM on shape 14, of 2 per SM on the pair kernel, of at most 4 per SM
+ *       as one shape-9 wave, else one more shape-10 wave;
  *   1, 2, 4 = ciphertexts (64 threads each) per CTA, key rows read from L2
  *       by every ciphertext;
  *   5 = 5 per CTA, key rows streamed once per CTA into a shared-memory ring
@@ -123,7 +123,12 @@ size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
  *       (two waves) in place of the pair kernel, whose two halves' partial
  *       products round differently; every launch then sums the key rows in
  *       the same order, and a ciphertext's result is the same bit for bit
- *       whatever batch it runs in (the gate server uses it).
+ *       whatever batch it runs in (the gate server uses it);
+ *   16 = the spread kernel over a cluster of two CTAs on two SMs: each CTA
+ *       holds one accumulator polynomial, runs its l forward transforms and
+ *       owns its output polynomial; transformed digits cross SMs through
+ *       distributed shared memory, one cluster barrier per step (lowest
+ *       latency: about 1.35 ms for a single gate's blind rotation).
  * FP64: 3 (L2) or 4 (ring, in line).  Engine tuning knob, no counterpart in
  * the reference (its kernel is a single HLS work-item). */
 tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,

@@ -2,8 +2,9 @@
 step for the roofline traffic, eager launch count) restates the engine's
 automatic split-FP32 shape (launch_auto_fp32 in csrc/bootstrap.cu, rule in
 include/tfhe_gpu.h): whole waves of 6 per SM on shape 10; a remainder of at
-most 1 per SM on the spread kernel, 2 per SM on the pair kernel, at most 4
-per SM as one shape-9 wave, else one more shape-10 wave.  CPU only."""
+most one per two SMs on the cluster spread kernel, at most 1 per SM on the
+spread kernel, 2 per SM on the pair kernel, at most 4 per SM as one shape-9
+wave, else one more shape-10 wave.  CPU only."""
 import os
 import sys
 
@@ -17,11 +18,14 @@ bench = pytest.importorskip("bench")
 PAIRS = "k_blind_rotate_ring<float,2,6,3,4,inline,nb2>"
 BATCHED = "k_blind_rotate_ring<float,2,4,3,4,inline,nb3>"
 SPREAD = "k_blind_rotate_spread<3>"
+SPREAD2 = "k_blind_rotate_spread2<3>"
 PAIR2 = "k_blind_rotate_pair<float,2,2,3,4>"
 
 
 @pytest.mark.parametrize("batch,want", [
-    (1, [SPREAD + " x 1"]),
+    (1, [SPREAD2 + " x 1"]),
+    (76, [SPREAD2 + " x 76"]),
+    (77, [SPREAD + " x 77"]),
     (152, [SPREAD + " x 152"]),
     (153, [PAIR2 + " x 153"]),
     (304, [PAIR2 + " x 304"]),
@@ -29,7 +33,8 @@ PAIR2 = "k_blind_rotate_pair<float,2,2,3,4>"
     (608, [BATCHED + " x 608"]),
     (609, [PAIRS]),
     (912, [PAIRS]),
-    (913, [PAIRS + " x 912", SPREAD + " x 1"]),
+    (913, [PAIRS + " x 912", SPREAD2 + " x 1"]),
+    (1064, [PAIRS + " x 912", SPREAD + " x 152"]),
     (1216, [PAIRS + " x 912", PAIR2 + " x 304"]),
     (1520, [PAIRS + " x 912", BATCHED + " x 608"]),
     (1521, [PAIRS]),
@@ -39,10 +44,17 @@ def test_automatic_shape_launches(batch, want):
     assert bench.blind_rotate_kernels("split_fp32", 0, batch) == want
 
 
+def test_fixed_order_shape_has_no_pair_kernel():
+    assert bench.blind_rotate_kernels("split_fp32", 15, 200) == [SPREAD + " x 200"]
+    assert bench.blind_rotate_kernels("split_fp32", 15, 912 + 60) == [PAIRS + " x 912", SPREAD2 + " x 60"]
+    assert bench.blind_rotate_kernels("split_fp32", 15, 4096) == bench.blind_rotate_kernels("split_fp32", 0, 4096)
+
+
 def test_explicit_shapes_and_other_set():
     assert bench.blind_rotate_kernels("split_fp32", 9, 100) == [BATCHED]
     assert bench.blind_rotate_kernels("split_fp32", 10, 100) == [PAIRS]
     assert bench.blind_rotate_kernels("split_fp32", 14, 5) == [SPREAD]
+    assert bench.blind_rotate_kernels("split_fp32", 16, 5) == [SPREAD2]
     assert bench.blind_rotate_kernels("split_fp32", 12, 5) == [PAIR2]
     assert bench.blind_rotate_kernels("split_fp32", 10, 100, l=2) == ["k_blind_rotate_ring<float,2,6,2,4,inline,nb2>"]
     assert bench.blind_rotate_kernels("fp64", 3, 100) == ["k_external_product<double,1,BlindRotate,3,3>"]

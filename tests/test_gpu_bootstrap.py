@@ -230,7 +230,8 @@ def test_errors_are_status_codes(pkg, keys, torch_cuda, P):
                                          ("split_fp32", 7), ("split_fp32", 8), ("split_fp32", 9),
                                          ("split_fp32", 10), ("split_fp32", 11), ("split_fp32", 12),
                                          ("split_fp32", 13), ("split_fp32", 14),
-                                         ("split_fp32", 15), ("fp64", 3), ("fp64", 4)])
+                                         ("split_fp32", 15), ("split_fp32", 16), ("fp64", 3),
+                                         ("fp64", 4)])
 def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, groups):
     """Each blind-rotation launch shape (L2-direct and shared-ring kernels) on
     a ragged batch: decrypted bits equal the truth and the oracle's, phases
@@ -415,10 +416,12 @@ def test_l2_shapes_have_no_waits(pkg, keys, torch_cuda):
         e.close()
 
 
-@pytest.mark.parametrize("count", [152, 153, 304, 305, 608, 609, 912, 913, 1064, 1065, 1216, 1217, 1520, 1521])
+@pytest.mark.parametrize("count", [76, 77, 152, 153, 304, 305, 608, 609, 912, 913, 988, 989, 1064, 1065, 1216,
+                                   1217, 1520, 1521])
 def test_auto_shape_boundaries(pkg, engine, oracle, keys, torch_cuda, P, count):
     """Batch sizes on both sides of the automatic shape's boundaries: the
-    spread kernel up to 1 per SM, the pair kernel up to 2 per SM; one
+    cluster spread kernel up to one per two SMs, the spread kernel up to 1
+    per SM, the pair kernel up to 2 per SM; one
     4-per-SM wave up to 4 per SM; 6-per-SM waves; a wave plus a spread tail,
     a pair tail, a 4-per-SM tail, or a partial 6-per-SM wave: every output
     decrypts to the truth."""
@@ -496,9 +499,10 @@ def test_stress_set_split_batches(pkg, torch_cuda, count):
 
 def test_shapes_agree_bit_for_bit(pkg, keys, torch_cuda, P, inputs):
     """Every split-FP32 shape that sums the 2l key rows in order (L2-direct
-    1/2/4, the rings 5-10, the spread kernel 14) runs the same transforms
-    and products in the same order, so their ciphertexts are identical bit
-    for bit.  The pair kernel adds the two halves' partial products and may
+    1/2/4, the rings 5-10, the spread kernel 14 and its two-SM cluster form
+    16, the fixed-order automatic shape 15) runs the same transforms and
+    products in the same order, so their ciphertexts are identical bit for
+    bit.  The pair kernel adds the two halves' partial products and may
     differ in the last rounding; it is held to the phase tolerance in the
     other tests."""
     torch = torch_cuda
@@ -510,7 +514,7 @@ def test_shapes_agree_bit_for_bit(pkg, keys, torch_cuda, P, inputs):
     try:
         e.upload_bootstrapping_key(keys["bk"], forms=("split_fp32",))
         e.upload_keyswitch_key(keys["ks"])
-        for shape in (1, 2, 4, 5, 6, 7, 8, 9, 10, 14, 15):
+        for shape in (1, 2, 4, 5, 6, 7, 8, 9, 10, 14, 15, 16):
             e.set_groups_per_cta("split_fp32", shape)
             d_out = torch.zeros((count, P.n + 1), dtype=torch.int32, device="cuda")
             e.bootsGates(gates, d_out, dev(torch, ca[:count]), dev(torch, cb[:count]), count, "split_fp32",
