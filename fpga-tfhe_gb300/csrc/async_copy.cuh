@@ -80,6 +80,46 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     }
     return true;
 }
+// ---- distributed shared memory (thread-block clusters) --------------------
+// Shared::cluster address of the same location in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t cluster_map(uint32_t local_smem, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local_smem), "r"(rank));
+    return r;
+}
+
+// Store 8 bytes into another CTA's shared memory; the bytes count as
+// transaction bytes on that CTA's mbarrier `rbar` when they land.
+__device__ __forceinline__ void st_async_f2(uint32_t raddr, float x, float y, uint32_t rbar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(raddr),
+                 "f"(x), "f"(y), "r"(rbar)
+                 : "memory");
+}
+
+// Wait (bounded, with the CTA's abort flag) for a phase of a barrier that
+// other CTAs of the cluster complete; acquire at cluster scope, so their
+// stores are visible afterwards.
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_cluster_bounded(uint64_t* bar, uint32_t parity,
+                                                          const volatile int* abort) {
+    if (mbar_try_wait_cluster(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait_cluster(bar, parity)) {
+        if (*abort || global_ns() - t0 > kWaitLimitNs) return false;
+    }
+    return true;
+}
+
 // Bulk copy global -> this CTA's shared memory; completion is counted in
 // bytes on `bar`.  dst, src 16-byte aligned; bytes a multiple of 16.
 // Start fetching `bytes` (a multiple of 16, 16-byte aligned) of global

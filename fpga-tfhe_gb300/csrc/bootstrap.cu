@@ -982,13 +982,20 @@ __global__ void __launch_bounds__(128 * L, 1) k_blind_rotate_spread(KParams kp, 
 // -- l local, l from the peer -- in row order with their part of each key
 // row, transform back, round and add into the local accumulator with
 // integer atomics.  The accumulator never crosses SMs, only 4 KB of digits
-// per group and step do.  The pushes alternate between two buffers, so the
-// one cluster barrier per step also orders a push after the peer's reads of
-// the buffer two steps back.  Each SM carries half the spread kernel's
-// shared-memory traffic and transforms; the products are summed in the same
-// order as every other shape, so the ciphertexts are bit-identical to the
-// spread kernel's.  Split-FP32 only, 1 CTA per SM (the shared-memory request
-// is padded so that the two CTAs take two SMs).
+// per group and step do.
+//
+// The pushes are asynchronous stores (st.async) that count their bytes on
+// the receiving CTA's mbarrier for that step: the owners wait (bounded) for
+// the peer's l x 4 KB to land, with no cluster-wide barrier and no release
+// fence on the sender.  Pushes alternate between two buffers, each with its
+// own mbarrier.  A push into buffer b at step k cannot overtake the peer's
+// reads of b at step k - 2: the pushing CTA has by then received the peer's
+// step k - 1 digits, which the peer sends only after its step k - 2
+// products.  Each SM carries half the spread kernel's shared-memory traffic
+// and transforms; the products are summed in the same order as every other
+// shape, so the ciphertexts are bit-identical to the spread kernel's.
+// Split-FP32 only, 1 CTA per SM (the shared-memory request is padded so
+// that the two CTAs take two SMs).
 // ----------------------------------------------------------------------
 template <int L>
 struct Spread2Plan {
@@ -998,7 +1005,8 @@ struct Spread2Plan {
     static constexpr size_t drem_off = dloc_off + L * kHalf * sizeof(cpx<float>);  // [buf][lev][q][t]
     static constexpr size_t scratch_off = drem_off + 2 * L * kHalf * sizeof(cpx<float>);
     static constexpr size_t scratch = 2 * kScratchStride * sizeof(cpx<float>);
-    static constexpr size_t total = scratch_off + L * scratch;
+    static constexpr size_t bar_off = scratch_off + L * scratch;  // 2 mbarriers, abort flag
+    static constexpr size_t total = bar_off + 2 * sizeof(uint64_t) + 16;
     static constexpr size_t request = total > 120 * 1024 ? total : 120 * 1024;  // one CTA per SM
 };
 
@@ -1017,7 +1025,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 * L, 1)
     int32_t* acc = reinterpret_cast<int32_t*>(smem + Plan::acc_off);
     cpx<float>* dloc = reinterpret_cast<cpx<float>*>(smem + Plan::dloc_off);
     cpx<float>* drem = reinterpret_cast<cpx<float>*>(smem + Plan::drem_off);
-    cpx<float>* drem_peer = cluster.map_shared_rank(drem, (unsigned)(r ^ 1));
+    uint64_t* dbar = reinterpret_cast<uint64_t*>(smem + Plan::bar_off);  // per buffer
+    volatile int* abort = reinterpret_cast<volatile int*>(smem + Plan::bar_off + 2 * sizeof(uint64_t));
+    // the peer's digit buffers and their mbarriers, as shared::cluster addresses
+    const uint32_t drem_peer = cluster_map(smem_u32(drem), (uint32_t)(r ^ 1));
+    const uint32_t dbar_peer = cluster_map(smem_u32(dbar), (uint32_t)(r ^ 1));
     const int c = blockIdx.x >> 1;
     const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
     const int lev = g;
@@ -1033,7 +1045,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 * L, 1)
         const int barb = mod_switch_2n(xs[n]);
         for (int i = threadIdx.x; i < kN; i += blockDim.x) acc[i] = r == 0 ? 0 : test_vector_coef(a, c, barb, i);
     }
-    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_init(&dbar[0], 1);
+        mbar_init(&dbar[1], 1);
+        *abort = 0;
+        fence_mbar_init();
+    }
+    cluster.sync();  // both CTAs' barriers initialised before any push
 
     const FftTwiddles<float> tw = hot_twiddles<float>(tables);
     const FftIdx ix = make_fft_idx(t);
@@ -1049,12 +1067,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 * L, 1)
     int a_next = bara ? bara[0] : mod_switch_2n(xs[0]);
     if (threadIdx.x < kRows && (threadIdx.x & 1) == r)
         bulk_prefetch_l2(gsw + (size_t)threadIdx.x * kRowElems, kRowElems * sizeof(cpx<float>));
-    int buf = 0;
+    uint32_t k = 0;  // steps taken (the same in both CTAs)
 #pragma unroll 1
     for (int i = 0; i < n; ++i) {
         const int ai = a_next;
         if (i + 1 < n) a_next = bara ? bara[i + 1] : mod_switch_2n(xs[i + 1]);
         if (ai == 0) continue;  // tfhe_blindRotate_FFT.cpp:114 (uniform over the cluster)
+        const int buf = (int)(k & 1);
+        // this step's incoming digits: one arrival and l x 4 KB of stores
+        if (threadIdx.x == 0) mbar_arrive_expect_tx(&dbar[buf], (uint32_t)(L * kHalf * sizeof(cpx<float>)));
         const cpx<float>* step_keys = gsw + (size_t)i * step_elems;
         if (i + 1 < n && threadIdx.x < kRows && (threadIdx.x & 1) == r)  // next step's rows into L2
             bulk_prefetch_l2(step_keys + step_elems + (size_t)threadIdx.x * kRowElems,
@@ -1080,11 +1101,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 * L, 1)
         fft512_forward_tw(v, sc, tw, ix, t, bar_id);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            dloc[(lev * 8 + q) * 64 + t] = v[q];
-            drem_peer[((buf * L + lev) * 8 + q) * 64 + t] = v[q];
+            const int e = (lev * 8 + q) * 64 + t;
+            dloc[e] = v[q];
+            st_async_f2(drem_peer + (uint32_t)((buf * L * kHalf + e) * sizeof(cpx<float>)), v[q].x, v[q].y,
+                        dbar_peer + (uint32_t)(buf * sizeof(uint64_t)));
         }
-        cluster.sync();  // every D of both polynomials in place; every read of acc done
+        __syncthreads();  // every local D in place; every read of acc done
         if (owner) {
+            if (!mbar_wait_cluster_bounded(&dbar[buf], (k >> 1) & 1, abort)) {  // the peer's D landed
+                *abort = 1;
+                atomicExch(a.err, 3);
+            }
             cpx<float> o[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q) o[q] = {0.f, 0.f};
@@ -1110,7 +1137,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 * L, 1)
                 atomicAdd(reinterpret_cast<unsigned*>(acc + x0 + kHalf), c1[q]);
             }
         }
-        buf ^= 1;
+        ++k;
         __syncthreads();  // the accumulator is updated before the next step reads it
     }
     if (a.acc_out) {
