@@ -128,7 +128,7 @@ struct Circuit {
     std::vector<int32_t> user_off, users;
     std::vector<int32_t> pending;
     std::vector<int64_t> wire_tick;      // tick that produces the wire (-1: an input)
-    std::vector<int8_t> wire_level;      // linear level within that tick (-1: a bootstrap)
+    std::vector<int32_t> wire_level;     // linear level within that tick (-1: a bootstrap)
     std::vector<double> produced;        // device completion time of the wire (s)
     int32_t unscheduled = 0;             // gates not yet in a tick
     double submitted = 0, admitted = 0, finished = 0;
@@ -343,7 +343,7 @@ void schedule(tfhe_gpu_server* s, Tick& T, int64_t k) {
             if ((int)T.lin.size() <= lvl) T.lin.resize(lvl + 1);
             T.lin[lvl].push_back(p);
             c->wire_tick[out] = k;
-            c->wire_level[out] = (int8_t)std::min(lvl, 127);
+            c->wire_level[out] = lvl;
             // a linear output is available within the tick
             release_users(c, p.g, [&](int32_t u) { s->ready.push_back({c, u}); });
         } else {

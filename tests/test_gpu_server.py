@@ -181,3 +181,27 @@ def test_burst_of_circuits_pipelined(pkg, engine, keys, circuits):
         assert (alone == outs[7]).all()
     finally:
         srv.close()
+
+
+def test_long_chain_of_linear_gates(pkg, engine, keys, circuits):
+    """200 NOT gates in a chain between two bootstrapped gates: the linear
+    gates of a tick run in levels (one launch per level), so a chain longer
+    than any small level counter still evaluates in order."""
+    P = pkg.default_params()
+    B = circuits.Builder(2)
+    w = B.gate(circuits.AND, 0, 1)
+    for _ in range(200):
+        w = B.gate(circuits.NOT, w)
+    out = B.gate(circuits.XOR, w, 0)
+    gates = B.array()
+    pkg.set_seed([85])
+    srv = pkg.Server(engine, pool_slots=1024, max_batch=64)
+    try:
+        for a, b in ((0, 0), (1, 1), (1, 0)):
+            ct = pkg.encrypt_bits(P, np.array([a, b], np.int32), keys["lwe"])
+            got = _run(srv, [(gates, 2, ct, [out])])[0]
+            want = circuits.evaluate(gates, np.array([a, b], np.int32), [out])
+            assert (pkg.decrypt_bits(P, got, keys["lwe"]) == want).all()
+            assert int(want[0]) == (a & b) ^ a  # 200 NOTs cancel
+    finally:
+        srv.close()
