@@ -978,7 +978,7 @@ __global__ void __launch_bounds__(128 * L, 1) k_blind_rotate_spread(KParams kp, 
 // (one per group) and owns output polynomial r (groups 0 and 1: the high and
 // the low key part).  Each group writes its transformed digits D_(r,lev) to
 // its own shared memory and pushes them into the peer CTA's (distributed
-// shared memory); after one cluster barrier the owners multiply all 2l rows
+// shared memory); once the peer's digits have landed the owners multiply all 2l rows
 // -- l local, l from the peer -- in row order with their part of each key
 // row, transform back, round and add into the local accumulator with
 // integer atomics.  The accumulator never crosses SMs, only 4 KB of digits

@@ -126,9 +126,10 @@ size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
  *       whatever batch it runs in (the gate server uses it);
  *   16 = the spread kernel over a cluster of two CTAs on two SMs: each CTA
  *       holds one accumulator polynomial, runs its l forward transforms and
- *       owns its output polynomial; transformed digits cross SMs through
- *       distributed shared memory, one cluster barrier per step (lowest
- *       latency: about 1.35 ms for a single gate's blind rotation).
+ *       owns its output polynomial; transformed digits cross SMs as
+ *       asynchronous stores into the peer's shared memory, counted on its
+ *       mbarrier (lowest latency: about 1.33 ms for a single gate's blind
+ *       rotation).
  * FP64: 3 (L2) or 4 (ring, in line).  Engine tuning knob, no counterpart in
  * the reference (its kernel is a single HLS work-item). */
 tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,
