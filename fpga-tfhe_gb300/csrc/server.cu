@@ -142,8 +142,6 @@ struct Pick {
 
 // One tick: what it runs, what it finishes, its events and staging.
 struct Tick {
-    int64_t index = -1;
-    bool busy = false;                          // enqueued, not yet retired
     std::vector<std::vector<Pick>> lin;         // linear gates by level
     std::vector<Pick> boot, mux;
     std::vector<Circuit*> finishing;            // circuits whose last gates are in this tick
@@ -286,7 +284,6 @@ tfhe_gpu_status retire_tick(tfhe_gpu_server* s, Tick& T) {
     T.mux.clear();
     T.finishing.clear();
     T.finishing_off.clear();
-    T.busy = false;
     ++s->next_retire;
     return TFHE_GPU_OK;
 }
@@ -519,7 +516,6 @@ tfhe_gpu_status enqueue(tfhe_gpu_server* s, Tick& T) {
         SCK(s, cudaMemcpyAsync(T.h_res, T.d_res, sizeof(int32_t) * n_res * W, cudaMemcpyDeviceToHost, st));
     }
     SCK(s, cudaEventRecord(T.end, st));
-    T.busy = true;
     s->gates_run += nb;
     return TFHE_GPU_OK;
 }
@@ -672,7 +668,6 @@ tfhe_gpu_status tfhe_gpu_server_step(tfhe_gpu_server* s, int32_t* ran) {
         admit(s);
     }
     Tick& T = s->ticks[s->next_tick % kInFlight];
-    T.index = s->next_tick;
     schedule(s, T, s->next_tick);
     int32_t n = (int32_t)(T.boot.size() + T.mux.size());
     for (auto& level : T.lin) n += (int32_t)level.size();
