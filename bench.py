@@ -840,6 +840,16 @@ def main():
         torch.cuda.synchronize()
         f64 = timed("fp64", 2)
         extras["fp64_batched_bootstraps_per_s"] = batch * 2 / (sum(f64) / 1000.0)
+        # the plain FP64 form's roofline: the same algorithmic work over the
+        # FP64 FMA-pipe peak measured now
+        f64_peak, f64_peak_ms = pkg.measure_fp64_peak(local)
+        f64_achieved = FLOP_PER_BOOTSTRAP * extras["fp64_batched_bootstraps_per_s"] / 1e12
+        extras["fp64_roofline"] = {
+            "bound": "fp64", "achieved": f64_achieved, "peak": f64_peak, "unit": "TFLOP/s",
+            "frac": f64_achieved / f64_peak,
+            "note": "whole FP64 gate step (blind rotation + key switch) per 162.6 MFLOP bootstrap; peak "
+                    "measured in this run by tfhe_gpu_measure_fp64_peak (independent FP64 FMA chains, "
+                    "%.1f ms)" % f64_peak_ms}
         # plain FP64 single-gate form (one gate per call), the >=10x denominator
         one_ms = []
         for s in range(4):

@@ -66,6 +66,15 @@ def measure_fp32_peak(device=0, iters=65536):
     return tf.value, ms.value
 
 
+def measure_fp64_peak(device=0, iters=2048):
+    """Measured FP64 FMA-pipe peak of the device: (TFLOP/s, probe ms)."""
+    tf, ms = ctypes.c_double(), ctypes.c_double()
+    st = lib().tfhe_gpu_measure_fp64_peak(int(device), int(iters), ctypes.byref(tf), ctypes.byref(ms))
+    if st:
+        raise TfheError(st, "measure_fp64_peak")
+    return tf.value, ms.value
+
+
 def default_params():
     """The reference's default gate set (constants.h:26-40)."""
     return Params(n=630, N=1024, k=1, l=3, Bgbit=7, ks_t=8, ks_basebit=2, split_bits=0,
@@ -161,6 +170,9 @@ SIGNATURES = {
     "tfhe_gpu_gate_keyset": (ctypes.c_int, [VP, I32P, I32P, I32P, I32P, ctypes.c_uint32]),
     "tfhe_gpu_selftest_timeout": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int32]),
     "tfhe_gpu_measure_fp32_peak": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32,
+                                                  ctypes.POINTER(ctypes.c_double),
+                                                  ctypes.POINTER(ctypes.c_double)]),
+    "tfhe_gpu_measure_fp64_peak": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32,
                                                   ctypes.POINTER(ctypes.c_double),
                                                   ctypes.POINTER(ctypes.c_double)]),
     "tfhe_client_set_seed": (None, [U32P, ctypes.c_int32]),

@@ -315,6 +315,10 @@ tfhe_gpu_status tfhe_gpu_selftest_timeout(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,
  * blind-rotation kernels' roofline is quoted against it.  No counterpart in
  * the reference.  iters = 65536 runs about 20 ms on a GB300. */
 tfhe_gpu_status tfhe_gpu_measure_fp32_peak(int32_t device, int32_t iters, double* tflops, double* ms);
+/* The same for the FP64 FMA pipe (independent FP64 FMA chains), the roof of
+ * the plain FP64 form.  No counterpart in the reference.  iters = 2048 runs
+ * about 30 ms on a GB300 (its FP64 rate is about 1/64 of its FP32 rate). */
+tfhe_gpu_status tfhe_gpu_measure_fp64_peak(int32_t device, int32_t iters, double* tflops, double* ms);
 
 /* ---- CUDA graph of a gate batch; launch-shape autotuner ----------------- */
 /* Capture the whole gate pipeline of one batch (combination, blind rotation

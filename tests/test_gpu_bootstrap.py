@@ -536,6 +536,13 @@ def test_fp32_peak_probe(pkg, torch_cuda):
     assert 40.0 <= tf <= 90.0, tf
 
 
+def test_fp64_peak_probe(pkg, torch_cuda):
+    """The FP64 FMA-pipe probe: GB300's FP64 rate is about 1/64 of FP32."""
+    tf, ms = pkg.measure_fp64_peak(0)
+    print("measured FP64 FMA peak: %.2f TFLOP/s (%.2f ms)" % (tf, ms))
+    assert 0.3 <= tf <= 5.0, tf
+
+
 @pytest.mark.parametrize("count", [200, 912 + 200])
 def test_fixed_order_shape_independent_of_batch(pkg, keys, torch_cuda, P, count):
     """Shape 15 (automatic, fixed summation order) gives every ciphertext the
