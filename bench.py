@@ -702,7 +702,14 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
         host_group = dist.new_group(backend="gloo")  # the host-side ciphertext gather
-    ge.build()
+    # one rank compiles (an up-to-date tree is left as it is); the others
+    # wait, so no two ranks write the same build files
+    if rank == 0:
+        ge.build()
+    if world > 1:
+        torch.distributed.barrier(group=host_group)
+    if rank != 0:
+        ge.build()
     pkg = ge.load_package()
     P = pkg.default_params()
     P.split_bits = args.split_bits
