@@ -12,10 +12,11 @@ seed 0, input bits from seed 4.  Synthetic data: no dataset is involved.
   e2e    -- the same metric through the host-buffer C entry point
             (tfhe_gpu_bootsGates_host): pinned host ciphertexts in, results
             out, copies inside the timed region.
-  roofline -- the dominant kernel (the blind-rotation kernel,
-            k_external_product<float,2,BlindRotate>) timed alone with CUDA
-            events: algorithmic FP work 162.6 MFLOP per bootstrap (FFT-form
-            count) over its duration, against the FP32 pipe peak.
+  roofline -- the dominant kernels (the blind-rotation launches of the
+            step, k_blind_rotate_ring for the 4096-gate layer) timed alone
+            with CUDA events: algorithmic FP work 162.6 MFLOP per bootstrap
+            (FFT-form count) over their duration, against the FP32 FMA-pipe
+            peak measured in the same run (tfhe_gpu_measure_fp32_peak).
   cpu_baseline -- the CPU oracle (restated reference path) on the host's
             cores on a bounded sample.
 
