@@ -576,3 +576,34 @@ def test_fixed_order_shape_independent_of_batch(pkg, keys, torch_cuda, P, count)
     names = sorted(pyoracle.GATES, key=lambda g: pyoracle.GATES[g])
     truth = np.array([pyoracle.GATE_FN[names[g]](x, y) for g, x, y in zip(gates, a, b)])
     assert (pkg.decrypt_bits(P, outs[0], keys["lwe"]) == truth).all()
+
+
+def test_cluster_spread_kernel_stress_set_bit_for_bit(pkg, torch_cuda):
+    """The two-SM cluster kernel (shape 16) on the l = 2 set gives the spread
+    kernel's (shape 14) ciphertexts bit for bit, and decrypts to the truth."""
+    torch = torch_cuda
+    P = pkg.stress_params()
+    lwe, tlwe, ks, bk = pkg.gate_keyset(P, [0])
+    count = 37
+    rng = np.random.default_rng(241)
+    a = rng.integers(0, 2, count)
+    b = rng.integers(0, 2, count)
+    pkg.set_seed([241])
+    d_a = torch.from_numpy(pkg.encrypt_bits(P, a, lwe)).cuda()
+    d_b = torch.from_numpy(pkg.encrypt_bits(P, b, lwe)).cuda()
+    e = pkg.Engine(P)
+    outs = {}
+    try:
+        e.upload_bootstrapping_key(bk, forms=("split_fp32",))
+        e.upload_keyswitch_key(ks)
+        for shape in (14, 16):
+            e.set_groups_per_cta("split_fp32", shape)
+            d_out = torch.empty_like(d_a)
+            e.bootsGate("NAND", d_out, d_a, d_b, count, "split_fp32", stream=cur(torch))
+            torch.cuda.synchronize()
+            e.synchronize()
+            outs[shape] = host(d_out)
+    finally:
+        e.close()
+    assert (outs[14] == outs[16]).all()
+    assert int((pkg.decrypt_bits(P, outs[16], lwe) != 1 - (a & b)).sum()) <= 1
