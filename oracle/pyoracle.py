@@ -1,6 +1,6 @@
 """ctypes binding of the CPU oracle (test infrastructure only).
 
-Loaded by tests/, by __graft_entry__.smoke() as the checker, and by the
+Loaded by tests/, by __graft_entry__.smoke() to check its result, and by the
 cpu_baseline / reference leg of bench.py.  The engine never imports this.
 """
 import ctypes

@@ -1,7 +1,7 @@
 """GPU parity of the blind rotation, the bootstrap and the gates against the
 CPU oracle, through the C ABI.
 
-Criteria (the north-star's): every decrypted gate output equals the oracle's
+Criteria: every decrypted gate output equals the oracle's
 and the plaintext truth; output phases agree with the oracle's within
 2^-6 of a turn (2^26 units).  Phases cannot agree more tightly in general:
 one rounding difference between two FFT implementations can move a gadget

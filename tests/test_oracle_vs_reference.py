@@ -1,6 +1,6 @@
 """The oracle against the reference's own code (oracle/_ref, built from the
 reference's sources by oracle/ref_pin/build_ref.py).  CPU only; skipped where
-the reference sources are not present (e.g. on the GPU machine).
+the reference sources are not present (no reference checkout on the machine).
 
 What is pinned, and how tightly:
   * numeric-functions.cpp (RNG, gaussian32, dtot32, modSwitch, approxPhase):
