@@ -127,6 +127,8 @@ SIGNATURES = {
     "tfhe_gpu_bootsMUX": (ctypes.c_int, [VP, VP, VP, VP, VP, ctypes.c_int32, ctypes.c_int, VP]),
     "tfhe_gpu_bootsGates_host": (ctypes.c_int, [VP, I32P, ctypes.c_int32, I32P, I32P, I32P,
                                                 ctypes.c_int32, ctypes.c_int]),
+    "tfhe_gpu_bootsGates_host_split": (ctypes.c_int, [ctypes.POINTER(VP), ctypes.c_int32, I32P, ctypes.c_int32,
+                                                      I32P, I32P, I32P, ctypes.c_int32, ctypes.c_int]),
     "tfhe_gpu_bootsGates_noalloc": (ctypes.c_int, [VP, VP, VP, VP, VP, ctypes.c_int32, ctypes.c_int,
                                                    VP]),
     "tfhe_gpu_server_create": (ctypes.c_int, [VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int,
@@ -709,6 +711,29 @@ class Engine:
                                                       ca.ctypes.data_as(I32P), cb.ctypes.data_as(I32P),
                                                       count, self._form(form)), "bootsGates_host")
         return out
+
+
+def bootsGates_host_split(engines, ca, cb, gates=None, gate="NAND", form="split_fp32", out=None):
+    """One layer of gates over several engines (tfhe_gpu_bootsGates_host_split):
+    contiguous shards, one per engine, run concurrently; outputs in layer
+    order.  The engines must be distinct and hold the same keys."""
+    ca = _np(ca, np.int32)
+    cb = _np(cb, np.int32)
+    if out is None:
+        out = np.zeros_like(ca)
+    gp = None
+    if gates is not None:
+        gates = _np(gates, np.int32)
+        gp = gates.ctypes.data_as(I32P)
+    arr = (VP * len(engines))(*[e.ctx for e in engines])
+    g = GATES[gate] if isinstance(gate, str) else int(gate)
+    st = lib().tfhe_gpu_bootsGates_host_split(arr, len(engines), gp, g, out.ctypes.data_as(I32P),
+                                              ca.ctypes.data_as(I32P), cb.ctypes.data_as(I32P), ca.shape[0],
+                                              Engine._form(form))
+    if st:
+        details = "; ".join(lib().tfhe_gpu_last_error(e.ctx).decode() for e in engines)
+        raise TfheError(st, "bootsGates_host_split: " + details)
+    return out
 
 
 class Server:

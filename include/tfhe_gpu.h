@@ -278,6 +278,20 @@ tfhe_gpu_status tfhe_gpu_bootsGates_host(tfhe_gpu_ctx* ctx, const int32_t* gates
                                          int32_t uniform_gate, int32_t* out,
                                          const int32_t* ca, const int32_t* cb,
                                          int32_t count, tfhe_gpu_form form);
+/* One circuit layer over several contexts -- normally one per GPU, each with
+ * its own copy of the keys (the reference partitions nothing; this is the
+ * engine's multi-GPU form of tfhe_gpu_bootsGates_host).  The `count` gates
+ * are cut into nctx contiguous shards of sizes differing by at most one,
+ * shard i runs on ctxs[i] through tfhe_gpu_bootsGates_host (one host thread
+ * per context, all concurrently), and writes its outputs into its slice of
+ * `out`, so the outputs come back in layer order.  The contexts must be
+ * distinct and share the parameter set; each is used by this call only
+ * until it returns.  On an error the first failing context's status is
+ * returned (tfhe_gpu_last_error of that context says why). */
+tfhe_gpu_status tfhe_gpu_bootsGates_host_split(tfhe_gpu_ctx* const* ctxs, int32_t nctx,
+                                               const int32_t* gates, int32_t uniform_gate,
+                                               int32_t* out, const int32_t* ca, const int32_t* cb,
+                                               int32_t count, tfhe_gpu_form form);
 /* Host-buffer form of tfhe_gpu_bootsMUX. */
 tfhe_gpu_status tfhe_gpu_bootsMUX_host(tfhe_gpu_ctx* ctx, int32_t* out, const int32_t* a,
                                        const int32_t* b, const int32_t* c, int32_t count,

@@ -607,3 +607,36 @@ def test_cluster_spread_kernel_stress_set_bit_for_bit(pkg, torch_cuda):
         e.close()
     assert (outs[14] == outs[16]).all()
     assert int((pkg.decrypt_bits(P, outs[16], lwe) != 1 - (a & b)).sum()) <= 1
+
+
+@pytest.mark.parametrize("count", [1000, 1])
+def test_layer_split_over_contexts(pkg, keys, torch_cuda, P, count):
+    """tfhe_gpu_bootsGates_host_split with two contexts (both on GPU 0 here,
+    one per GPU in use): the shards run concurrently and the outputs come
+    back in layer order, bit-identical to the whole layer on one context
+    (fixed summation order, shape 15); a 1-gate layer leaves one context an
+    empty shard; the same context twice is refused."""
+    rng = np.random.default_rng(251)
+    a = rng.integers(0, 2, count)
+    b = rng.integers(0, 2, count)
+    gates = rng.integers(0, 10, count).astype(np.int32)
+    pkg.set_seed([251])
+    ca = pkg.encrypt_bits(P, a, keys["lwe"])
+    cb = pkg.encrypt_bits(P, b, keys["lwe"])
+    engines = [pkg.Engine(pkg.default_params()) for _ in range(3)]
+    try:
+        for e in engines:
+            e.upload_bootstrapping_key(keys["bk"], forms=("split_fp32",))
+            e.upload_keyswitch_key(keys["ks"])
+            e.set_groups_per_cta("split_fp32", 15)
+        whole = engines[0].bootsGates_host(ca, cb, gates=gates)
+        split = pkg.bootsGates_host_split(engines[1:], ca, cb, gates=gates)
+        assert (split == whole).all()
+        names = sorted(pyoracle.GATES, key=lambda g: pyoracle.GATES[g])
+        truth = np.array([pyoracle.GATE_FN[names[g]](x, y) for g, x, y in zip(gates, a, b)])
+        assert (pkg.decrypt_bits(P, split, keys["lwe"]) == truth).all()
+        with pytest.raises(pkg.TfheError):
+            pkg.bootsGates_host_split([engines[1], engines[1]], ca, cb, gates=gates)
+    finally:
+        for e in engines:
+            e.close()
