@@ -86,6 +86,8 @@ def parse():
     ap.add_argument("--rate", type=float, default=8.0, help="requests/s per client (serve)")
     ap.add_argument("--groups", type=int, default=0,
                     help="ciphertexts per CTA of the split-FP32 blind rotation (0 = engine default)")
+    ap.add_argument("--layers", type=int, default=245,
+                    help="chained 4096-gate layers of the failures workload (245: about 10^6 gates)")
     ap.add_argument("--replicas", action="store_true",
                     help="N > 1: every rank runs the whole layer (weak scaling) instead of a shard of it")
     ap.add_argument("--no-extras", action="store_true",
@@ -558,15 +560,16 @@ def run_failures(torch, pkg, eng, P, lwe, width=4096, layers=245, form="split_fp
 
 def workload_failures(args, world, rank, local):
     """10^6 gate bootstraps (default set, split-FP32) as 245 chained layers of
-    4096 random gates, decryption checked (one JSON line)."""
+    4096 random gates (--layers for more), decryption checked (one JSON
+    line)."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
     P = pkg.default_params()
     P.split_bits = args.split_bits
     torch, pkg, eng, keys, stream = _engine_setup(P, [0], local, forms=("split_fp32",))
-    r = run_failures(torch, pkg, eng, P, keys[0])
+    r = run_failures(torch, pkg, eng, P, keys[0], layers=args.layers)
     line = {"metric": "decryption failures", "value": r["failures"], "unit": "failures",
-            "gates": r["gates"], "n_gpus": 1, "steps": 245, "warmup": 0,
+            "gates": r["gates"], "n_gpus": 1, "steps": args.layers, "warmup": 0,
             "ms_per_step": r["gpu_ms_per_layer"], "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "%d gate bootstraps: " % r["gates"] + r["workload"]},
