@@ -55,6 +55,7 @@ DRAM_KEY_BYTES_PER_LAUNCH = 61.9e6
 DRAM_IO_BYTES_PER_BOOTSTRAP = 2.52e3 + 4.5e3
 BATCH = 4096
 GATE_SET = (0, 1, 3, 2)           # NAND, AND, XOR, OR
+GATE_NAMES = {0: "NAND", 1: "AND", 2: "OR", 3: "XOR"}
 L2_FLUSH_BYTES = 256 << 20
 SMS = 152
 FP32_LANES_PER_SM = 128
@@ -242,6 +243,8 @@ def cpu_baseline(seconds, batch_hint):
     a = rng.integers(0, 2, n)
     b = rng.integers(0, 2, n)
     gates = np.array(GATE_SET, np.int32)[rng.integers(0, len(GATE_SET), n)]
+    want = np.array([pyoracle.GATE_FN[name](x, y) for name, x, y in
+                     zip([GATE_NAMES[g] for g in gates], a, b)])
     o.set_seed([4])
     ca = o.encrypt_bits(P, a, lwe)
     cb = o.encrypt_bits(P, b, lwe)
@@ -265,7 +268,41 @@ def cpu_baseline(seconds, batch_hint):
             "sample": "%d gate bootstraps (mixed NAND/AND/XOR/OR, default set) in %.1f s on %d threads"
                       % (done, el, threads),
             "single_core": {"bootstraps_per_s": one / el1, "gate_latency_ms": 1000.0 * el1 / one,
-                            "sample": "%d gates one after another on 1 thread in %.1f s" % (one, el1)}}
+                            "sample": "%d gates one after another on 1 thread in %.1f s" % (one, el1)},
+            "fast_cpu": cpu_fast_baseline(P, bk, ks, gates, ca, cb, want, threads, seconds / 2, o, lwe)}
+
+
+def cpu_fast_baseline(P, bk, ks, gates, ca, cb, want, threads, seconds, o, lwe):
+    """The same gates through the faster CPU bootstrap (N/2-point twisted
+    transform, the upstream library's method) on all host cores and on one:
+    the CPU figure without the reference's 2N-point transform.  Its
+    decrypted bits are checked against the plaintext truth `want`."""
+    from oracle import pyoracle
+    fast = pyoracle.CpuFast(P, bk, ks)
+    try:
+        done, t0 = 0, time.perf_counter()
+        while True:
+            out = fast.boots_gates(gates, ca, cb, threads)
+            done += len(gates)
+            el = time.perf_counter() - t0
+            if el >= seconds:
+                break
+        wrong = int((o.decrypt_bits(P, out, lwe) != want).sum())
+        one, t1 = 0, time.perf_counter()
+        while True:
+            fast.boots_gates(gates[:1], ca[:1], cb[:1], 1)
+            one += 1
+            el1 = time.perf_counter() - t1
+            if el1 >= min(3.0, seconds / 2):
+                break
+    finally:
+        fast.close()
+    return {"bootstraps_per_s": done / el, "cores": threads,
+            "gate_latency_ms_one_core": 1000.0 * el1 / one, "wrong": wrong,
+            "method": "N/2-point twisted complex transform in FP64 (the upstream TFHE library's method), "
+                      "radix-2, split real/imaginary arrays, one gate per thread",
+            "sample": "%d gates in %.1f s on %d threads; %d gates on 1 thread in %.1f s"
+                      % (done, el, threads, one, el1)}
 
 
 def run_reference(args, world, rank):

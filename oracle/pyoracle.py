@@ -352,6 +352,52 @@ class Oracle:
         return out
 
 
+class CpuFast:
+    """The faster CPU gate bootstrap (oracle/tfhe_cpu_fast.cpp): the same
+    gates with the N/2-point twisted transform in double precision, for the
+    timed CPU comparison only.  Holds the key in its transform domain; the
+    key-switching key array is referenced, not copied, and is kept alive
+    here."""
+
+    def __init__(self, P, bk, ks, lib_path=None):
+        if lib_path is None:
+            lib_path = build_oracle.build_fast()
+        self.lib = ctypes.CDLL(lib_path)
+        self.lib.cpuf_create.restype = ctypes.c_void_p
+        self.lib.cpuf_create.argtypes = [ctypes.POINTER(Params), I32P, I32P]
+        self.lib.cpuf_destroy.restype = None
+        self.lib.cpuf_destroy.argtypes = [ctypes.c_void_p]
+        self.lib.cpuf_boots_gates.restype = None
+        self.lib.cpuf_boots_gates.argtypes = [ctypes.c_void_p, I32P, I32P, I32P, I32P, ctypes.c_int32,
+                                              ctypes.c_int32]
+        self.P = P
+        self._ks = np.ascontiguousarray(ks, np.int32)
+        bk = np.ascontiguousarray(bk, np.int32)
+        self.h = self.lib.cpuf_create(ctypes.byref(P), _p(bk, I32P), _p(self._ks, I32P))
+        if not self.h:
+            raise ValueError("cpuf_create refused the parameters")
+
+    def boots_gates(self, gates, ca, cb, threads=0):
+        gates = np.ascontiguousarray(gates, np.int32)
+        ca = np.ascontiguousarray(ca, np.int32)
+        cb = np.ascontiguousarray(cb, np.int32)
+        out = np.zeros_like(ca)
+        self.lib.cpuf_boots_gates(self.h, _p(gates, I32P), _p(ca, I32P), _p(cb, I32P), _p(out, I32P),
+                                  len(gates), int(threads))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cpuf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 _ORACLE = None
 
 
