@@ -17,8 +17,13 @@ seed 0, input bits from seed 4.  Synthetic data: no dataset is involved.
             with CUDA events: algorithmic FP work 162.6 MFLOP per bootstrap
             (FFT-form count) over their duration, against the FP32 FMA-pipe
             peak measured in the same run (tfhe_gpu_measure_fp32_peak).
+  roofline_smem -- the same kernels against the resource that bounds them:
+            shared-memory wavefronts per bootstrap (ncu counts of the same
+            kernels) over their duration, against one wavefront per SM clock.
   cpu_baseline -- the CPU oracle (restated reference path) on the host's
-            cores on a bounded sample.
+            cores on a bounded sample; beside it (fast_cpu) the same gates
+            through a CPU bootstrap with the upstream library's N/2-point
+            transform (oracle/tfhe_cpu_fast.cpp).
 
 `--impl reference` times the reference's CPU path instead (the oracle
 restatement; the upstream library the reference links is not available) and
@@ -52,6 +57,15 @@ FLOP_PER_BOOTSTRAP = 162.6e6      # FFT-form algorithmic count, default set
 # ciphertext moves 2.5 KB in and 4.5 KB out (66.5 MB measured for one
 # 608-gate wave of the batched ring kernel, 66.2 MB by this rule).
 DRAM_KEY_BYTES_PER_LAUNCH = 61.9e6
+# Shared-memory wavefronts per bootstrap of the two batched ring kernels
+# (the shared-memory wavefront count of a full ncu capture of each: 1.58 G
+# for a 912-gate wave, 0.74 G for a 448-gate wave; the capture is
+# summarised in profiles/blind_rotate_ring_pairs_batched_keyswitch_batch1360.md).
+# The shared-memory pipe serves one wavefront per SM clock.
+SMEM_WAVEFRONTS_PER_BOOTSTRAP = {
+    "k_blind_rotate_ring<float,2,6,3,4,inline,nb2>": 1.58e9 / 912,
+    "k_blind_rotate_ring<float,2,4,3,4,inline,nb3>": 0.74e9 / 448,
+}
 DRAM_IO_BYTES_PER_BOOTSTRAP = 2.52e3 + 4.5e3
 BATCH = 4096
 GATE_SET = (0, 1, 3, 2)           # NAND, AND, XOR, OR
@@ -176,11 +190,17 @@ def make_inputs(pkg, P, lwe_key, batch, seed=4):
 
 
 class ClockSampler:
-    """nvidia-smi samples of SM clock / throttle reasons during the timed region."""
+    """nvidia-smi samples of SM clock / throttle reasons during the timed
+    region: entering starts nvidia-smi and waits (up to 3 s) for its first
+    sample, so that the sampler is live when the timed work starts; the
+    summary uses the samples taken after that one."""
+
+    INTERVAL_MS = 100
 
     def __init__(self, index):
         self.index = index
         self.lines = []
+        self.first = 0
         self.proc = None
 
     def __enter__(self):
@@ -190,9 +210,13 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.INTERVAL_MS)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.perf_counter()
+            while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.005)
+            self.first = len(self.lines)
         except OSError:
             self.proc = None
         return self
@@ -212,7 +236,8 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines[self.first:] or self.lines
+        for ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 7:
                 continue
@@ -1043,6 +1068,8 @@ def main():
                                                                                      clk_peak.summary().get("sm_mhz")),
                          "nominal_peak": nominal_peak,
                          "frac_of_nominal": achieved / nominal_peak},
+            "roofline_smem": smem_roofline(blind_rotate_kernels(args.form, eng.get_groups_per_cta(args.form),
+                                                                batch), batch, k_ms, clocks),
             "clocks": clocks,
         }
         line.update(extras)
@@ -1103,6 +1130,26 @@ def side_paths(pkg, torch, eng, P, keys, d_ca, d_cb, batch, stream, sp):
         e2.close()
     out["cloud_key_file"] = {"bytes": size, "save_s": t_save, "load_to_device_s": t_load}
     return out
+
+
+def smem_roofline(kernels, batch, k_ms, clocks):
+    """The blind rotation against the resource that bounds it: shared-memory
+    wavefronts (ncu counts per bootstrap of the same kernels) over the
+    kernels' time in this run, against one wavefront per SM clock at the SM
+    clock sampled during the timed region.  None when a kernel of the step
+    has no counted figure."""
+    total = 0.0
+    for name in kernels:
+        base, _, cnt = name.partition(" x ")
+        if base not in SMEM_WAVEFRONTS_PER_BOOTSTRAP:
+            return None
+        total += SMEM_WAVEFRONTS_PER_BOOTSTRAP[base] * (int(cnt) if cnt else batch)
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    achieved = total / (k_ms / 1000.0) / 1e9
+    peak = SMS * mhz * 1e6 / 1e9
+    return {"bound": "shared-memory pipe", "achieved": achieved, "peak": peak, "unit": "G wavefronts/s",
+            "frac": achieved / peak, "wavefronts_per_step": total,
+            "note": "wavefronts per bootstrap from ncu counts of the same kernels, time from this run"}
 
 
 def blind_rotate_kernels(form, shape, batch, l=3):

@@ -58,3 +58,17 @@ def test_explicit_shapes_and_other_set():
     assert bench.blind_rotate_kernels("split_fp32", 12, 5) == [PAIR2]
     assert bench.blind_rotate_kernels("split_fp32", 10, 100, l=2) == ["k_blind_rotate_ring<float,2,6,2,4,inline,nb2>"]
     assert bench.blind_rotate_kernels("fp64", 3, 100) == ["k_external_product<double,1,BlindRotate,3,3>"]
+
+
+def test_shared_memory_roofline_counts_each_kernel_part():
+    kernels = bench.blind_rotate_kernels("split_fp32", 0, 4096)
+    r = bench.smem_roofline(kernels, 4096, 31.0, {"sm_mhz": 2000.0})
+    want = 3648 * 1.58e9 / 912 + 448 * 0.74e9 / 448
+    assert abs(r["wavefronts_per_step"] - want) < 1.0
+    assert abs(r["achieved"] - want / 0.031 / 1e9) < 1e-6
+    assert abs(r["peak"] - 152 * 2000.0 / 1000.0) < 1e-9
+    # one whole-batch launch of a counted kernel
+    r = bench.smem_roofline([PAIRS], 912, 6.6, None)
+    assert abs(r["wavefronts_per_step"] - 1.58e9) < 1.0
+    # a step with a kernel that has no count gives no figure
+    assert bench.smem_roofline(bench.blind_rotate_kernels("split_fp32", 0, 100), 100, 1.3, None) is None
