@@ -203,7 +203,10 @@ __device__ __forceinline__ FftTwiddles<R> hot_twiddles(const cpx<R>* hot) {
 //   RingKeys   -- from a shared-memory ring filled by a producer warp with
 //                 bulk copies (see k_blind_rotate_ring).
 // FB digit polynomials are transformed together (fft512_forward_tw_multi), and
-// IB parts of an output polynomial are transformed back together.
+// IB parts of an output polynomial are transformed back together.  IP: the
+// in-place transforms (fft512_forward_ip / fft512_inverse_ip: one group
+// barrier per transform instead of two), alternating the two exchange
+// buffers of each stream from one transform to the next.
 // ----------------------------------------------------------------------
 template <typename R, int PARTS, int NB>
 struct StepCtx {
@@ -266,11 +269,11 @@ __device__ __forceinline__ void mac_row(cpx<R> (&out)[2][PARTS][8], const cpx<R>
 
 // Levels lev0 .. lev0 + NBK - 1 of input polynomial jp: digits, NBK forward
 // transforms run together, and their key rows multiply-accumulated.
-template <int NBK, typename R, int PARTS, int NB, typename Keys>
+template <int NBK, bool IP, typename R, int PARTS, int NB, typename Keys>
 __device__ __forceinline__ void forward_levels(const StepCtx<R, PARTS, NB>& S, Keys& keys,
                                                cpx<R> (&out)[2][PARTS][8], const uint32_t (&r0)[8],
                                                const uint32_t (&r1)[8], int p0, int lev0, uint32_t mask,
-                                               int halfBg) {
+                                               int halfBg, int which) {
     const int t = S.t;
     cpx<R> v[NBK][8];
 #pragma unroll
@@ -281,8 +284,15 @@ __device__ __forceinline__ void forward_levels(const StepCtx<R, PARTS, NB>& S, K
             v[b][r] = digit_pair<R>(r0[r], r1[r], decal, mask, halfBg);
         }
     }
-    fft512_forward_tw_multi<NBK>(v, *reinterpret_cast<const FftScratch<R>(*)[NBK]>(S.s), S.tw, S.ix, t,
-                                 S.bar_id);
+    if constexpr (IP) {
+        cpx<R>* x[NBK];
+#pragma unroll
+        for (int b = 0; b < NBK; ++b) x[b] = which ? S.s[b].b1 : S.s[b].b0;
+        fft512_forward_ip<NBK>(v, x, S.tw, S.ix, t, S.bar_id);
+    } else {
+        fft512_forward_tw_multi<NBK>(v, *reinterpret_cast<const FftScratch<R>(*)[NBK]>(S.s), S.tw, S.ix, t,
+                                     S.bar_id);
+    }
 #pragma unroll
     for (int b = 0; b < NBK; ++b) {
         const int p = p0 + lev0 + b;
@@ -291,7 +301,7 @@ __device__ __forceinline__ void forward_levels(const StepCtx<R, PARTS, NB>& S, K
     }
 }
 
-template <typename R, int PARTS, bool ROT, int L, int FB, int IB, int NB, typename Keys>
+template <typename R, int PARTS, bool ROT, int L, int FB, int IB, int NB, bool IP = false, typename Keys>
 __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& keys, int a) {
     static_assert(PARTS % IB == 0 && FB <= NB && IB <= NB, "batch sizes");
     const int t = S.t;
@@ -305,6 +315,7 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
         for (int pt = 0; pt < PARTS; ++pt)
 #pragma unroll
             for (int q = 0; q < 8; ++q) out[j][pt][q] = {(R)0, (R)0};
+    int which = 0;  // IP: the exchange buffer of the next transform
 
 #pragma unroll 1
     for (int jp = 0; jp < 2; ++jp) {
@@ -326,10 +337,14 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
         }
         // blocks of FB levels, then the remaining L % FB together
 #pragma unroll
-        for (int lev0 = 0; lev0 + FB <= L; lev0 += FB)
-            forward_levels<FB>(S, keys, out, r0, r1, jp * L, lev0, mask, halfBg);
-        if constexpr (L % FB != 0)
-            forward_levels<L % FB>(S, keys, out, r0, r1, jp * L, L - L % FB, mask, halfBg);
+        for (int lev0 = 0; lev0 + FB <= L; lev0 += FB) {
+            forward_levels<FB, IP>(S, keys, out, r0, r1, jp * L, lev0, mask, halfBg, which);
+            which ^= 1;
+        }
+        if constexpr (L % FB != 0) {
+            forward_levels<L % FB, IP>(S, keys, out, r0, r1, jp * L, L - L % FB, mask, halfBg, which);
+            which ^= 1;
+        }
     }
 
     // back to the coefficient domain (j unrolled: out[j] must stay in registers)
@@ -344,8 +359,16 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
             for (int b = 0; b < IB; ++b)
 #pragma unroll
                 for (int q = 0; q < 8; ++q) v[b][q] = out[j][pt0 + b][q];
-            fft512_inverse_tw_multi<IB>(v, *reinterpret_cast<const FftScratch<R>(*)[IB]>(S.s), S.tw, S.ix, t,
-                                        S.bar_id);
+            if constexpr (IP) {
+                cpx<R>* x[IB];
+#pragma unroll
+                for (int b = 0; b < IB; ++b) x[b] = which ? S.s[b].b1 : S.s[b].b0;
+                fft512_inverse_ip<IB>(v, x, S.tw, S.ix, t, S.bar_id);
+            } else {
+                fft512_inverse_tw_multi<IB>(v, *reinterpret_cast<const FftScratch<R>(*)[IB]>(S.s), S.tw, S.ix,
+                                            t, S.bar_id);
+            }
+            which ^= 1;
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
 #pragma unroll
@@ -456,12 +479,14 @@ __device__ __forceinline__ void add_part(cpx<R> (&out)[2][PARTS][8], const cpx<R
 
 // The fused step of the shared-ring kernel, with one copy of each transform
 // in the code: the levels and the (output, part) pairs are run-time loops
-// (a fully unrolled step overflows the instruction cache).
+// (a fully unrolled step overflows the instruction cache).  In-place
+// transforms, alternating the two exchange buffers.
 template <typename R, int PARTS, int L, typename Keys>
 __device__ __forceinline__ void ep_step_lean(const StepCtx<R, PARTS, 1>& S, Keys& keys, int a) {
     const int t = S.t;
     const int halfBg = 1 << (S.Bgbit - 1);
     const uint32_t mask = (1u << S.Bgbit) - 1;
+    int which = 0;  // the exchange buffer of the next transform
 
     cpx<R> out[2][PARTS][8];
 #pragma unroll
@@ -488,7 +513,8 @@ __device__ __forceinline__ void ep_step_lean(const StepCtx<R, PARTS, 1>& S, Keys
 #pragma unroll
             for (int r = 0; r < 8; ++r)
                 v[r] = digit_pair<R>(r0[r], r1[r], decal, mask, halfBg);
-            fft512_forward_tw(v, S.s[0], S.tw, S.ix, t, S.bar_id);
+            fft512_forward_ip1(v, which ? S.s[0].b1 : S.s[0].b0, S.tw, S.ix, t, S.bar_id);
+            which ^= 1;
             const int p = jp * L + lev;
             mac_row<R, PARTS, Keys::kShared>(out, v, keys.acquire(p), t);
             keys.release(p);
@@ -501,7 +527,8 @@ __device__ __forceinline__ void ep_step_lean(const StepCtx<R, PARTS, 1>& S, Keys
         const int j = u / PARTS, pt = u % PARTS;
         cpx<R> v[8];
         pick_part<R, PARTS>(v, out, j, pt);
-        fft512_inverse_tw(v, S.s[0], S.tw, S.ix, t, S.bar_id);
+        fft512_inverse_ip1(v, which ? S.s[0].b1 : S.s[0].b0, S.tw, S.ix, t, S.bar_id);
+        which ^= 1;
         round_part<R, PARTS>(v, pt, S.split, c0, c1);
         if (pt == PARTS - 1) {
             int32_t* dst = S.acc + j * kN;
@@ -721,7 +748,9 @@ struct RingPlan {
 // NB = 1: one transform at a time (ep_step_lean).  NB > 1: the l forward
 // and the PARTS inverse transforms of a step run together (ep_step), which
 // needs NB exchange buffer pairs per group and about 250 registers, so at
-// most four groups per CTA.
+// most four groups per CTA.  NB <= 2 uses the in-place transforms (one group
+// barrier per transform; measured faster), NB = 3 the two-barrier form (the
+// in-place form took its 608-gate wave from 4.57 to 4.90 ms).
 template <typename R, int PARTS, int GROUPS, int L, int S, bool INLINE, int NB = 1>
 __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
     k_blind_rotate_ring(KParams kp, Tables T, EpArgs a) {
@@ -810,7 +839,7 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
             continue;
         }
         if constexpr (NB == 1) ep_step_lean<R, PARTS, L>(St, keys, ai);
-        else ep_step<R, PARTS, true, L, (NB < L ? NB : L), PARTS, NB>(St, keys, ai);
+        else ep_step<R, PARTS, true, L, (NB < L ? NB : L), PARTS, NB, (NB <= 2)>(St, keys, ai);
     }
     if (keys.producer) keys.drain();
     if (a.acc_out) {
@@ -927,7 +956,7 @@ __global__ void __launch_bounds__(128 * L, 1) k_blind_rotate_spread(KParams kp, 
                 v[r] = digit_pair<float>(u0, u1, decal, mask, halfBg);
             }
         }
-        fft512_forward_tw(v, sc, tw, ix, t, bar_id);
+        fft512_forward_ip1(v, sc.b0, tw, ix, t, bar_id);
 #pragma unroll
         for (int q = 0; q < 8; ++q) dsh[(g * 8 + q) * 64 + t] = v[q];
         __syncthreads();  // every D written, every read of acc done
@@ -944,7 +973,7 @@ __global__ void __launch_bounds__(128 * L, 1) k_blind_rotate_spread(KParams kp, 
                     o[2 * qq] = cmac(o[2 * qq], d0, cpx<float>{kk[p][qq].x, kk[p][qq].y});
                     o[2 * qq + 1] = cmac(o[2 * qq + 1], d1, cpx<float>{kk[p][qq].z, kk[p][qq].w});
                 }
-            fft512_inverse_tw(o, sc, tw, ix, t, bar_id);
+            fft512_inverse_ip1(o, sc.b0, tw, ix, t, bar_id);
             uint32_t c0[8] = {}, c1[8] = {};  // the low part adds into them
             round_part<float, 2>(o, opt, kp.split, c0, c1);
             int32_t* dst = acc + oj * kN;
@@ -1098,7 +1127,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 * L, 1)
             const uint32_t u1 = (uint32_t)rot_coef(acc, x0 + kHalf, ai) - (uint32_t)acc[x0 + kHalf] + kp.offset;
             v[q] = digit_pair<float>(u0, u1, decal, mask, halfBg);
         }
-        fft512_forward_tw(v, sc, tw, ix, t, bar_id);
+        fft512_forward_ip1(v, sc.b0, tw, ix, t, bar_id);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int e = (lev * 8 + q) * 64 + t;
@@ -1127,7 +1156,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 * L, 1)
                     o[2 * qq + 1] = cmac(o[2 * qq + 1], d1, cpx<float>{kk[p][qq].z, kk[p][qq].w});
                 }
             }
-            fft512_inverse_tw(o, sc, tw, ix, t, bar_id);
+            fft512_inverse_ip1(o, sc.b0, tw, ix, t, bar_id);
             uint32_t c0[8] = {}, c1[8] = {};  // the low part adds into them
             round_part<float, 2>(o, opt, kp.split, c0, c1);
 #pragma unroll

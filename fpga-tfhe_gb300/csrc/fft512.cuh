@@ -440,6 +440,123 @@ __device__ __forceinline__ void fft512_inverse_tw(cpx<R> (&v)[8], const FftScrat
                                *reinterpret_cast<const FftScratch<R>(*)[1]>(&s), tw, ix, t, bar_id);
 }
 
+// ----------------------------------------------------------------------
+// In-place forms: one exchange buffer per transform.  Pass B reads and
+// writes the same positions of a thread, and the exchange between passes B
+// and C stays within groups of 8 consecutive lanes (position 8t + r is
+// written by lane 8(t/8) + r), so it needs only __syncwarp; the exchange
+// between passes A and B crosses the two warps and keeps the group barrier.
+// A caller that runs two transforms on one buffer with no group barrier
+// between them would race (the second's pass A writes against the first's
+// pass C reads in the other warp): it alternates two buffers instead.  The
+// arithmetic is that of fft512_forward_tw_multi / fft512_inverse_tw_multi,
+// bit for bit.
+// ----------------------------------------------------------------------
+template <int NB, typename R>
+__device__ __forceinline__ void fft512_forward_ip(cpx<R> (&v)[NB][8], cpx<R>* const (&x)[NB],
+                                                  const FftTwiddles<R>& tw, const FftIdx& ix, int t,
+                                                  int bar_id) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 1; r < 8; ++r) v[b][r] = cmul(v[b][r], twist_c<R>(r));
+        dft8<1>(v[b]);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const cpx<R> w = tw.a[q * 64 + t];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) v[b][q] = cmul(v[b][q], w);
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[b][slot_a<R>(ix, t, q)] = v[b][q];
+    group_sync(bar_id);
+    const int j = t & 7;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[b][r] = x[b][slot_b<R>(ix, t, r)];
+        dft8<1>(v[b]);
+    }
+#pragma unroll
+    for (int q = 1; q < 8; ++q) {
+        const cpx<R> w = tw.b[q * 8 + j];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) v[b][q] = cmul(v[b][q], w);
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[b][slot_b<R>(ix, t, q)] = v[b][q];
+    __syncwarp();
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[b][r] = x[b][slot_c<R>(ix, t, r)];
+        dft8<1>(v[b]);
+    }
+}
+
+template <int NB, typename R>
+__device__ __forceinline__ void fft512_inverse_ip(cpx<R> (&v)[NB][8], cpx<R>* const (&x)[NB],
+                                                  const FftTwiddles<R>& tw, const FftIdx& ix, int t,
+                                                  int bar_id) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        dft8<-1>(v[b]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[b][slot_c<R>(ix, t, q)] = v[b][q];
+    }
+    __syncwarp();
+    const int j = t & 7;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        if (r == 0) {
+#pragma unroll
+            for (int b = 0; b < NB; ++b) v[b][0] = x[b][slot_b<R>(ix, t, 0)];
+        } else {
+            const cpx<R> w = tw.b[r * 8 + j];
+#pragma unroll
+            for (int b = 0; b < NB; ++b) v[b][r] = cmulc(x[b][slot_b<R>(ix, t, r)], w);
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        dft8<-1>(v[b]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[b][slot_b<R>(ix, t, q)] = v[b][q];
+    }
+    group_sync(bar_id);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const cpx<R> w = tw.a[r * 64 + t];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) v[b][r] = cmulc(x[b][slot_a<R>(ix, t, r)], w);
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        dft8<-1>(v[b]);
+#pragma unroll
+        for (int q = 1; q < 8; ++q) v[b][q] = cmulc(v[b][q], twist_c<R>(q));
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void fft512_forward_ip1(cpx<R> (&v)[8], cpx<R>* x, const FftTwiddles<R>& tw,
+                                                   const FftIdx& ix, int t, int bar_id) {
+    cpx<R>* const xs[1] = {x};
+    fft512_forward_ip<1>(*reinterpret_cast<cpx<R>(*)[1][8]>(&v), xs, tw, ix, t, bar_id);
+}
+
+template <typename R>
+__device__ __forceinline__ void fft512_inverse_ip1(cpx<R> (&v)[8], cpx<R>* x, const FftTwiddles<R>& tw,
+                                                   const FftIdx& ix, int t, int bar_id) {
+    cpx<R>* const xs[1] = {x};
+    fft512_inverse_ip<1>(*reinterpret_cast<cpx<R>(*)[1][8]>(&v), xs, tw, ix, t, bar_id);
+}
+
 // Frequency held at (thread t, register q) after the forward transform.
 __host__ __device__ __forceinline__ int freq_of(int t, int q) {
     return (t >> 3) + 8 * (t & 7) + 64 * q;
