@@ -206,7 +206,9 @@ __device__ __forceinline__ FftTwiddles<R> hot_twiddles(const cpx<R>* hot) {
 // IB parts of an output polynomial are transformed back together.  IP: the
 // in-place transforms (fft512_forward_ip / fft512_inverse_ip: one group
 // barrier per transform instead of two), alternating the two exchange
-// buffers of each stream from one transform to the next.
+// buffers of each stream from one transform to the next.  EARLY: a block's
+// key rows are tested for arrival before its forward transforms and waited
+// for after them.
 // ----------------------------------------------------------------------
 template <typename R, int PARTS, int NB>
 struct StepCtx {
@@ -230,6 +232,8 @@ struct GlobalKeys {
             asm volatile("prefetch.global.L1 [%0];" ::"l"(gb + (size_t)ln * 128));
     }
     __device__ __forceinline__ const cpx<R>* acquire(int p) const { return gsw + (size_t)p * kRow; }
+    __device__ __forceinline__ bool poll(int) const { return true; }
+    __device__ __forceinline__ const cpx<R>* acquire_polled(int p, bool) const { return acquire(p); }
     __device__ __forceinline__ void release(int) const {}
     static constexpr bool kShared = false;
 };
@@ -269,12 +273,15 @@ __device__ __forceinline__ void mac_row(cpx<R> (&out)[2][PARTS][8], const cpx<R>
 
 // Levels lev0 .. lev0 + NBK - 1 of input polynomial jp: digits, NBK forward
 // transforms run together, and their key rows multiply-accumulated.
-template <int NBK, bool IP, typename R, int PARTS, int NB, typename Keys>
+template <int NBK, bool IP, bool EARLY, typename R, int PARTS, int NB, typename Keys>
 __device__ __forceinline__ void forward_levels(const StepCtx<R, PARTS, NB>& S, Keys& keys,
                                                cpx<R> (&out)[2][PARTS][8], const uint32_t (&r0)[8],
                                                const uint32_t (&r1)[8], int p0, int lev0, uint32_t mask,
                                                int halfBg, int which) {
     const int t = S.t;
+    bool landed[NBK];
+#pragma unroll
+    for (int b = 0; b < NBK; ++b) landed[b] = EARLY ? keys.poll(p0 + lev0 + b) : false;
     cpx<R> v[NBK][8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
@@ -296,12 +303,14 @@ __device__ __forceinline__ void forward_levels(const StepCtx<R, PARTS, NB>& S, K
 #pragma unroll
     for (int b = 0; b < NBK; ++b) {
         const int p = p0 + lev0 + b;
-        mac_row<R, PARTS, Keys::kShared>(out, v[b], keys.acquire(p), t);
+        mac_row<R, PARTS, Keys::kShared>(out, v[b], EARLY ? keys.acquire_polled(p, landed[b]) : keys.acquire(p),
+                                         t);
         keys.release(p);
     }
 }
 
-template <typename R, int PARTS, bool ROT, int L, int FB, int IB, int NB, bool IP = false, typename Keys>
+template <typename R, int PARTS, bool ROT, int L, int FB, int IB, int NB, bool IP = false, bool EARLY = false,
+          typename Keys>
 __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& keys, int a) {
     static_assert(PARTS % IB == 0 && FB <= NB && IB <= NB, "batch sizes");
     const int t = S.t;
@@ -338,11 +347,11 @@ __device__ __forceinline__ void ep_step(const StepCtx<R, PARTS, NB>& S, Keys& ke
         // blocks of FB levels, then the remaining L % FB together
 #pragma unroll
         for (int lev0 = 0; lev0 + FB <= L; lev0 += FB) {
-            forward_levels<FB, IP>(S, keys, out, r0, r1, jp * L, lev0, mask, halfBg, which);
+            forward_levels<FB, IP, EARLY>(S, keys, out, r0, r1, jp * L, lev0, mask, halfBg, which);
             which ^= 1;
         }
         if constexpr (L % FB != 0) {
-            forward_levels<L % FB, IP>(S, keys, out, r0, r1, jp * L, L - L % FB, mask, halfBg, which);
+            forward_levels<L % FB, IP, EARLY>(S, keys, out, r0, r1, jp * L, L - L % FB, mask, halfBg, which);
             which ^= 1;
         }
     }
@@ -729,6 +738,20 @@ struct RingKeys {
         if (!mbar_wait_bounded(&full[slot], (r / S) & 1, abort)) give_up();
         return ring + slot * kRow;
     }
+    // acquire() in two parts, so that the arrival test's round trip overlaps
+    // other work: poll() issues rows (producer) and tests once whether row p
+    // has landed; acquire_polled() waits (bounded) only if it had not.
+    __device__ __forceinline__ bool poll(int p) {
+        const uint32_t r = row0 + (uint32_t)p;
+        if (producer) issue_upto(r);
+        return mbar_try_wait(&full[r % S], (r / S) & 1);
+    }
+    __device__ __forceinline__ const cpx<R>* acquire_polled(int p, bool landed) {
+        const uint32_t r = row0 + (uint32_t)p;
+        const uint32_t slot = r % S;
+        if (!landed && !mbar_wait_bounded(&full[slot], (r / S) & 1, abort)) give_up();
+        return ring + slot * kRow;
+    }
     // per_warp: one lane arrives for its whole warp once the warp has read
     // the row (the slot's count is then the number of consumer warps); else
     // every consumer thread arrives
@@ -767,8 +790,10 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
     k_blind_rotate_ring(KParams kp, Tables T, EpArgs a) {
     using Plan = RingPlan<R, PARTS, GROUPS, L, S, NB>;
     constexpr int kpl = 2 * L;
-    // measured: the two-at-a-time form is faster with one slot release per
-    // consumer warp (6.48 -> 6.45 ms per 912-gate wave), the others are not
+    // measured on the two-at-a-time form (NB = 2), not faster for the others:
+    // one slot release per consumer warp (6.48 -> 6.45 ms per 912-gate wave)
+    // and the rows' arrival tested before the transforms (6.45 -> 6.41 ms;
+    // the 4-per-SM form went from 4.58 to 4.98 ms with it)
     constexpr bool kPerWarp = NB == 2;
     extern __shared__ __align__(128) char smem[];
     cpx<R>* tables = reinterpret_cast<cpx<R>*>(smem);
@@ -853,7 +878,7 @@ __global__ void __launch_bounds__(64 * GROUPS + (INLINE ? 0 : 32), 1)
             continue;
         }
         if constexpr (NB == 1) ep_step_lean<R, PARTS, L>(St, keys, ai);
-        else ep_step<R, PARTS, true, L, (NB < L ? NB : L), PARTS, NB, (NB <= 2)>(St, keys, ai);
+        else ep_step<R, PARTS, true, L, (NB < L ? NB : L), PARTS, NB, (NB <= 2), kPerWarp>(St, keys, ai);
     }
     if (keys.producer) keys.drain();
     if (a.acc_out) {
