@@ -99,6 +99,8 @@ def parse():
     ap.add_argument("--clients", type=int, default=64)
     ap.add_argument("--requests", type=int, default=8, help="requests per client (serve)")
     ap.add_argument("--rate", type=float, default=8.0, help="requests/s per client (serve)")
+    ap.add_argument("--pool-slots", type=int, default=131072,
+                    help="ciphertext slots of the server's device pool (serve)")
     ap.add_argument("--groups", type=int, default=0,
                     help="ciphertexts per CTA of the split-FP32 blind rotation (0 = engine default)")
     ap.add_argument("--stress-gates", type=int, default=65536, help="NAND gates of the stress workload")
@@ -747,7 +749,7 @@ def workload_serve(args, world, rank, local):
     reqs, total_boots = serving_requests(pkg, P, lwe, args.clients, args.requests, args.rate)
     result = {}
     for form in args.serve_forms.split(","):
-        result[form] = run_serving(pkg, eng, P, lwe, reqs, total_boots, form)
+        result[form] = run_serving(pkg, eng, P, lwe, reqs, total_boots, form, pool_slots=args.pool_slots)
     first = args.serve_forms.split(",")[0]
     f = result[first]
     line = {"metric": "gate bootstraps/sec (serving)", "value": f["bootstraps_per_s"],
