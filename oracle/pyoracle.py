@@ -104,6 +104,8 @@ class Oracle:
             "orc_gate_combine": (None, [PP, ctypes.c_int32, I32P, I32P, I32P]),
             "orc_boots_gate": (None, [PP, F64P, I32P, ctypes.c_int32, I32P, I32P, I32P]),
             "orc_boots_mux": (None, [PP, F64P, I32P, I32P, I32P, I32P, I32P]),
+            "orc_boots_mux_batch": (None, [PP, F64P, I32P, I32P, I32P, I32P, I32P, ctypes.c_int32,
+                                           ctypes.c_int32]),
             "orc_boots_gate_batch": (None, [PP, F64P, I32P, I32P, I32P, I32P, I32P,
                                             ctypes.c_int32, ctypes.c_int32]),
             "orc_extern_mul_exact_batch": (None, [PP, I32P, I32P, ctypes.c_int32, ctypes.c_int32]),
@@ -289,6 +291,17 @@ class Oracle:
                                _p(np.ascontiguousarray(a, np.int32), I32P),
                                _p(np.ascontiguousarray(b, np.int32), I32P),
                                _p(np.ascontiguousarray(c, np.int32), I32P), _p(out, I32P))
+        return out
+
+    def boots_mux_batch(self, P, bk_fft, ks, a, b, c, threads=0):
+        """bootsMUX of count triples of samples (each count x (n+1)) on
+        `threads` host threads (0: all)."""
+        a = np.ascontiguousarray(a, np.int32)
+        b = np.ascontiguousarray(b, np.int32)
+        c = np.ascontiguousarray(c, np.int32)
+        out = np.zeros_like(a)
+        self.lib.orc_boots_mux_batch(ctypes.byref(P), _p(bk_fft, F64P), _p(ks, I32P), _p(a, I32P), _p(b, I32P),
+                                     _p(c, I32P), _p(out, I32P), len(a), int(threads))
         return out
 
     def test_vector(self, N, table):

@@ -749,6 +749,22 @@ void orc_boots_mux(const orc_params* P, const double* bk_fft,
     orc_keyswitch(P, ks, s.data(), out);
 }
 
+/* `count` independent bootsMUX (above) on `threads` OpenMP threads. */
+void orc_boots_mux_batch(const orc_params* P, const double* bk_fft,
+                         const int32_t* ks, const int32_t* a, const int32_t* b,
+                         const int32_t* c, int32_t* out, int32_t count,
+                         int32_t threads) {
+    const int32_t w = P->n + 1;
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
+#endif
+    for (int32_t g = 0; g < count; ++g)
+        orc_boots_mux(P, bk_fft, ks, a + (size_t)g * w, b + (size_t)g * w,
+                      c + (size_t)g * w, out + (size_t)g * w);
+    (void)threads;
+}
+
 void orc_boots_gate_batch(const orc_params* P, const double* bk_fft,
                           const int32_t* ks, const int32_t* gates,
                           const int32_t* ca, const int32_t* cb, int32_t* out,

@@ -147,6 +147,11 @@ void orc_boots_gate(const orc_params* P, const double* bk_fft,
 void orc_boots_mux(const orc_params* P, const double* bk_fft,
                    const int32_t* ks, const int32_t* a, const int32_t* b,
                    const int32_t* c, int32_t* out);
+/* count independent bootsMUX on `threads` OpenMP threads (<= 0: all). */
+void orc_boots_mux_batch(const orc_params* P, const double* bk_fft,
+                         const int32_t* ks, const int32_t* a, const int32_t* b,
+                         const int32_t* c, int32_t* out, int32_t count,
+                         int32_t threads);
 /* a batch of independent gates on `threads` OpenMP threads */
 void orc_boots_gate_batch(const orc_params* P, const double* bk_fft,
                           const int32_t* ks, const int32_t* gates,

@@ -399,3 +399,104 @@ def test_external_products_1024_against_exact(engine, oracle, keys, torch_cuda, 
                                                   log2_turn(rms), float((d == 0).mean())))
         assert np.abs(d).max() <= max_tol
         assert rms <= rms_tol
+
+
+# ---------------------------------------------------------------------------
+# the paths either side of the gate bootstrap at size: bootsMUX and the
+# programmable bootstrap, default set, both forms
+# ---------------------------------------------------------------------------
+def noise_stats_check(tag, form, d, e_gpu, e_ref, sigma_tol):
+    """Print and check the engine-vs-oracle phase statistics of one workload:
+    the same noise sigma within sampling error, no bias, no heavier tail."""
+    s_gpu, s_ref, s_d = e_gpu.std(), e_ref.std(), d.std()
+    print("\n[%s, %s] " % (tag, form) + describe("engine - oracle", d))
+    print("[%s, %s] output noise sigma: engine 2^%.3f, oracle 2^%.3f turn (ratio %.4f); max |noise| engine "
+          "2^%.2f, oracle 2^%.2f" % (tag, form, log2_turn(s_gpu), log2_turn(s_ref), s_gpu / s_ref,
+                                     log2_turn(np.abs(e_gpu).max()), log2_turn(np.abs(e_ref).max())))
+    assert 1 - sigma_tol <= s_gpu / s_ref <= 1 + sigma_tol, (s_gpu, s_ref)
+    assert abs(d.mean()) <= 5 * s_d / np.sqrt(len(d))
+    assert s_d <= (1 + sigma_tol) * np.hypot(s_gpu, s_ref)
+    assert np.abs(e_gpu).max() <= 1.25 * max(np.abs(e_ref).max(), 6 * s_ref)
+    assert np.abs(d).max() < 2 ** 28
+
+
+@pytest.fixture(scope="module")
+def mux_set(oracle, keys, P):
+    """1,024 bootsMUX (2,048 bootstraps) on random select/input bits, and the
+    oracle's on every host thread."""
+    rng = np.random.default_rng(41)
+    count = 1024
+    bits = rng.integers(0, 2, (3, count))
+    oracle.set_seed([41])
+    enc = [oracle.encrypt_bits(P, bits[i], keys["lwe"]) for i in range(3)]
+    ref = oracle.boots_mux_batch(P, keys["bk_fft"], keys["ks"], enc[0], enc[1], enc[2])
+    return {"enc": enc, "ref": ref, "truth": np.where(bits[0] == 1, bits[1], bits[2])}
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_mux_1024_against_oracle(engine, oracle, keys, torch_cuda, P, mux_set, form):
+    """All 1,024 MUX outputs decrypt like the oracle's and the truth, with the
+    oracle's output-noise distribution (sigma within 12 %: 1,024 samples)."""
+    torch = torch_cuda
+    count = len(mux_set["truth"])
+    e = mux_set["enc"]
+    d_out = torch.zeros((count, P.n + 1), dtype=torch.int32, device="cuda")
+    engine.bootsMUX(d_out, dev(torch, e[0]), dev(torch, e[1]), dev(torch, e[2]), count, form, stream=cur(torch))
+    torch.cuda.synchronize()
+    engine.synchronize()
+    got = d_out.cpu().numpy()
+    bits = oracle.decrypt_bits(P, got, keys["lwe"])
+    ref_bits = oracle.decrypt_bits(P, mux_set["ref"], keys["lwe"])
+    assert (ref_bits == mux_set["truth"]).all()
+    assert (bits == mux_set["truth"]).all(), int((bits != mux_set["truth"]).sum())
+    ph = oracle.phases(got, keys["lwe"], P.n)
+    ph_ref = oracle.phases(mux_set["ref"], keys["lwe"], P.n)
+    noise_stats_check("bootsMUX 1024", form, wrap_diff(ph, ph_ref).astype(np.float64), output_noise(ph, bits),
+                      output_noise(ph_ref, ref_bits), 0.12)
+
+
+LUT_P = 8  # messages of the lookup-table workload (padded: phase m / 16)
+
+
+def lut_decode(phases, p):
+    """Padded message of Torus32 phases: round(phase * 2p) mod 2p."""
+    ph = np.asarray(phases, np.int64) & 0xFFFFFFFF
+    return ((ph * 2 * p + (1 << 31)) >> 32) % (2 * p)
+
+
+@pytest.fixture(scope="module")
+def lut_set(pkg, oracle, keys, P):
+    """1,024 programmable bootstraps of random messages m < 8 through the
+    table f(m) = 5m + 3 mod 8, and the oracle's on every host thread."""
+    rng = np.random.default_rng(43)
+    count = 1024
+    m = rng.integers(0, LUT_P, count)
+    f = (5 * np.arange(LUT_P) + 3) % LUT_P
+    table = np.array([pkg.mod_switch_to_torus32(int(v), 2 * LUT_P) for v in f], np.int32)
+    tv = oracle.test_vector(P.N, table)
+    pkg.set_seed([43])
+    x = pkg.encrypt_phases(P, [pkg.mod_switch_to_torus32(int(v), 2 * LUT_P) for v in m], keys["lwe"])
+    ref = oracle.bootstrap_tv_batch(P, keys["bk_fft"], keys["ks"], tv, x)
+    ideal = np.array([pkg.mod_switch_to_torus32(int(v), 2 * LUT_P) for v in f[m]], np.int64)
+    return {"x": x, "tv": tv, "ref": ref, "want": f[m], "ideal": ideal}
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_lookup_table_1024_against_oracle(engine, oracle, keys, torch_cuda, P, lut_set, form):
+    """All 1,024 programmable bootstraps decode to the table's value, like the
+    oracle's, with the oracle's output-noise distribution."""
+    torch = torch_cuda
+    count = len(lut_set["want"])
+    d_x = dev(torch, lut_set["x"])
+    d_out = torch.zeros_like(d_x)
+    engine.bootstrap_tv(d_out, d_x, dev(torch, lut_set["tv"]), count, form, stream=cur(torch))
+    torch.cuda.synchronize()
+    engine.synchronize()
+    got = d_out.cpu().numpy()
+    ph = oracle.phases(got, keys["lwe"], P.n)
+    ph_ref = oracle.phases(lut_set["ref"], keys["lwe"], P.n)
+    assert (lut_decode(ph_ref, LUT_P) == lut_set["want"]).all()
+    assert (lut_decode(ph, LUT_P) == lut_set["want"]).all()
+    e_gpu = wrap_diff(ph, lut_set["ideal"]).astype(np.float64)
+    e_ref = wrap_diff(ph_ref, lut_set["ideal"]).astype(np.float64)
+    noise_stats_check("lookup table 1024", form, wrap_diff(ph, ph_ref).astype(np.float64), e_gpu, e_ref, 0.12)

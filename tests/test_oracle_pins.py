@@ -159,6 +159,16 @@ def test_mux_truth_table(oracle, P, keys):
                 assert oracle.decrypt_bits(P, out, keys["lwe"])[0] == (b if a else c)
 
 
+def test_mux_batch_is_the_single_mux(oracle, P, keys):
+    """The threaded bootsMUX batch gives, word for word, the single call's
+    results (same code per item, any thread)."""
+    oracle.set_seed([23])
+    a, b, c = (oracle.encrypt_bits(P, bits, keys["lwe"]) for bits in ([1, 0, 1], [0, 1, 1], [1, 1, 0]))
+    got = oracle.boots_mux_batch(P, keys["bk_fft"], keys["ks"], a, b, c)
+    for i in range(3):
+        assert (got[i] == oracle.boots_mux(P, keys["bk_fft"], keys["ks"], a[i], b[i], c[i])).all()
+
+
 def test_blind_rotate_fft_vs_exact_small_n(oracle):
     """Full blind rotation, FP64 transform against the exact integer product,
     on a shortened LWE dimension so that the exact path is quick.  Compared
