@@ -1158,7 +1158,9 @@ def blind_rotate_kernels(form, shape, batch, l=3):
     """Names of the blind-rotation kernels a launch of `batch` runs with
     launch shape `shape` (the engine's dispatch rules)."""
     if form == "fp64":
-        return (["k_external_product<double,1,BlindRotate,3,%d>" % l] if shape == 3
+        if shape == 16 or (shape == 0 and batch <= SMS // 2):
+            return ["k_blind_rotate_spread2_f64<%d>" % l]
+        return (["k_external_product<double,1,BlindRotate,3,%d>" % l] if shape in (0, 3)
                 else ["k_blind_rotate_ring<double,1,4,%d,4,inline>" % l])
     ring = "k_blind_rotate_ring<float,2,%d,%d,4,%s>"
     batched = "k_blind_rotate_ring<float,2,4,%d,4,inline,nb%d>" % (l, max(l, 2))

@@ -96,6 +96,14 @@ __device__ __forceinline__ void st_async_f2(uint32_t raddr, float x, float y, ui
                  : "memory");
 }
 
+// The same for 16 bytes (two doubles, as four 32-bit words).
+__device__ __forceinline__ void st_async_d2(uint32_t raddr, double x, double y, uint32_t rbar) {
+    asm volatile(
+        "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(raddr),
+        "r"(__double2loint(x)), "r"(__double2hiint(x)), "r"(__double2loint(y)), "r"(__double2hiint(y)), "r"(rbar)
+        : "memory");
+}
+
 // Wait (bounded, with the CTA's abort flag) for a phase of a barrier that
 // other CTAs of the cluster complete; acquire at cluster scope, so their
 // stores are visible afterwards.

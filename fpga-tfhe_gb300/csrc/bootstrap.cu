@@ -1227,6 +1227,179 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 * L, 1)
 }
 
 // ----------------------------------------------------------------------
+// The FP64 form's blind rotation over a cluster of two CTAs (lowest FP64
+// latency).  The same split as k_blind_rotate_spread2: CTA r holds
+// accumulator polynomial r and runs its l forward transforms (one per group),
+// pushes the transformed digits into the peer's shared memory (asynchronous
+// stores counted on the peer's mbarrier, two alternating buffers), and owns
+// output polynomial r.  The FP64 key has one part, so one owner group per
+// CTA (group 0) multiplies all 2l rows in row order with output r's part of
+// each key row, transforms back and truncates like the reference
+// (TorusPolynomial_fft.cpp:40).  The transforms, the products and their
+// order are those of the other FP64 shapes.  A single FP64 gate then runs on
+// two SMs' FP64 pipes instead of one 64-thread group.
+// ----------------------------------------------------------------------
+template <int L>
+struct Spread2F64Plan {
+    static constexpr size_t tables = kHotSize * sizeof(cpx<double>);
+    static constexpr size_t acc_off = tables;                                       // own polynomial
+    static constexpr size_t dloc_off = acc_off + kN * sizeof(int32_t);             // [lev][q][t]
+    static constexpr size_t drem_off = dloc_off + L * kHalf * sizeof(cpx<double>);  // [buf][lev][q][t]
+    static constexpr size_t scratch_off = drem_off + 2 * L * kHalf * sizeof(cpx<double>);
+    static constexpr size_t scratch = 2 * kScratchStride * sizeof(cpx<double>);
+    static constexpr size_t bar_off = scratch_off + L * scratch;  // 2 mbarriers, abort flag
+    static constexpr size_t total = bar_off + 2 * sizeof(uint64_t) + 16;
+    static constexpr size_t request = total > 120 * 1024 ? total : 120 * 1024;  // one CTA per SM
+    static_assert(dloc_off % 16 == 0 && drem_off % 16 == 0 && bar_off % 8 == 0, "alignment");
+};
+
+template <int L>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 * L, 1)
+    k_blind_rotate_spread2_f64(KParams kp, Tables T, EpArgs a) {
+    namespace cg = cooperative_groups;
+    using Plan = Spread2F64Plan<L>;
+    constexpr int kRows = 2 * L;
+    constexpr int kRowElems = 2 * kHalf;  // complex values per key row (two outputs, one part)
+    constexpr int kEarly = L;             // rows whose key values the owner loads before the transform
+    extern __shared__ __align__(128) char smem[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int r = (int)cluster.block_rank();  // this CTA's polynomial
+    cpx<double>* tables = reinterpret_cast<cpx<double>*>(smem);
+    int32_t* acc = reinterpret_cast<int32_t*>(smem + Plan::acc_off);
+    cpx<double>* dloc = reinterpret_cast<cpx<double>*>(smem + Plan::dloc_off);
+    cpx<double>* drem = reinterpret_cast<cpx<double>*>(smem + Plan::drem_off);
+    uint64_t* dbar = reinterpret_cast<uint64_t*>(smem + Plan::bar_off);  // per buffer
+    volatile int* abort = reinterpret_cast<volatile int*>(smem + Plan::bar_off + 2 * sizeof(uint64_t));
+    const uint32_t drem_peer = cluster_map(smem_u32(drem), (uint32_t)(r ^ 1));
+    const uint32_t dbar_peer = cluster_map(smem_u32(dbar), (uint32_t)(r ^ 1));
+    const int c = blockIdx.x >> 1;
+    const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
+    const int lev = g;
+    const bool owner = g == 0;
+    const int n = kp.n;
+    load_hot_tables<double>(tables, T);
+    if (a.acc_in) {
+        const int32_t* src = a.acc_in + (size_t)c * 2 * kN + (size_t)r * kN;
+        for (int i = threadIdx.x; i < kN; i += blockDim.x) acc[i] = src[i];
+    } else {
+        const int32_t* xs = a.x + (size_t)c * (n + 1);
+        const int barb = mod_switch_2n(xs[n]);
+        for (int i = threadIdx.x; i < kN; i += blockDim.x) acc[i] = r == 0 ? 0 : test_vector_coef(a, c, barb, i);
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&dbar[0], 1);
+        mbar_init(&dbar[1], 1);
+        *abort = 0;
+        fence_mbar_init();
+    }
+    cluster.sync();  // both CTAs' barriers initialised before any push
+
+    const FftTwiddles<double> tw = hot_twiddles<double>(tables);
+    const FftIdx ix = make_fft_idx(t);
+    const FftScratch<double> sc = scratch_at<double>(smem + Plan::scratch_off + (size_t)g * Plan::scratch);
+    const int bar_id = 1 + g;
+    const int halfBg = 1 << (kp.Bgbit - 1);
+    const uint32_t mask = (1u << kp.Bgbit) - 1;
+    const int decal = 32 - (lev + 1) * kp.Bgbit;
+    const cpx<double>* gsw = reinterpret_cast<const cpx<double>*>(a.gsw);
+    const size_t step_elems = (size_t)kRows * kRowElems;
+    const int32_t* bara = a.bara ? a.bara + (size_t)c * n : nullptr;
+    const int32_t* xs = a.x ? a.x + (size_t)c * (n + 1) : nullptr;
+    int a_next = bara ? bara[0] : mod_switch_2n(xs[0]);
+    if (threadIdx.x < kRows)  // output r's part of the first step's rows into L2
+        bulk_prefetch_l2(gsw + (size_t)threadIdx.x * kRowElems + r * kHalf, kHalf * sizeof(cpx<double>));
+    uint32_t k = 0;  // steps taken (the same in both CTAs)
+#pragma unroll 1
+    for (int i = 0; i < n; ++i) {
+        const int ai = a_next;
+        if (i + 1 < n) a_next = bara ? bara[i + 1] : mod_switch_2n(xs[i + 1]);
+        if (ai == 0) continue;  // tfhe_blindRotate_FFT.cpp:114 (uniform over the cluster)
+        const int buf = (int)(k & 1);
+        // this step's incoming digits: one arrival and l x 8 KB of stores
+        if (threadIdx.x == 0) mbar_arrive_expect_tx(&dbar[buf], (uint32_t)(L * kHalf * sizeof(cpx<double>)));
+        const cpx<double>* step_keys = gsw + (size_t)i * step_elems;
+        if (i + 1 < n && threadIdx.x < kRows)  // the next step's rows into L2
+            bulk_prefetch_l2(step_keys + step_elems + (size_t)threadIdx.x * kRowElems + r * kHalf,
+                             kHalf * sizeof(cpx<double>));
+        // the owner's first rows go out before the transform, so their L2
+        // latency overlaps it
+        double2 kk[kEarly][8];
+        if (owner) {
+#pragma unroll
+            for (int p = 0; p < kEarly; ++p) {
+                const double2* g2 = reinterpret_cast<const double2*>(step_keys + (size_t)p * kRowElems + r * kHalf);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) kk[p][q] = __ldg(g2 + key_index<double>(t, q));
+            }
+        }
+        cpx<double> v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int x0 = t + 64 * q;
+            const uint32_t u0 = (uint32_t)rot_coef(acc, x0, ai) - (uint32_t)acc[x0] + kp.offset;
+            const uint32_t u1 = (uint32_t)rot_coef(acc, x0 + kHalf, ai) - (uint32_t)acc[x0 + kHalf] + kp.offset;
+            v[q] = digit_pair<double>(u0, u1, decal, mask, halfBg);
+        }
+        fft512_forward_ip1(v, sc.b0, tw, ix, t, bar_id);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int e = (lev * 8 + q) * 64 + t;
+            dloc[e] = v[q];
+            st_async_d2(drem_peer + (uint32_t)((buf * L * kHalf + e) * sizeof(cpx<double>)), v[q].x, v[q].y,
+                        dbar_peer + (uint32_t)(buf * sizeof(uint64_t)));
+        }
+        __syncthreads();  // every local D in place; every read of acc done
+        if (owner) {
+            if (!mbar_wait_cluster_bounded(&dbar[buf], (k >> 1) & 1, abort)) {  // the peer's D landed
+                *abort = 1;
+                atomicExch(a.err, 3);
+            }
+            cpx<double> o[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) o[q] = {0.0, 0.0};
+#pragma unroll
+            for (int p = 0; p < kRows; ++p) {
+                const int jp = p / L, lv = p - jp * L;
+                const cpx<double>* D = jp == r ? dloc + lv * kHalf : drem + (buf * L + lv) * kHalf;
+                const double2* g2 = reinterpret_cast<const double2*>(step_keys + (size_t)p * kRowElems + r * kHalf);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const double2 w = p < kEarly ? kk[p < kEarly ? p : 0][q] : __ldg(g2 + key_index<double>(t, q));
+                    o[q] = cmac(o[q], D[q * 64 + t], cpx<double>{w.x, w.y});
+                }
+            }
+            fft512_inverse_ip1(o, sc.b0, tw, ix, t, bar_id);
+            uint32_t c0[8], c1[8];
+            round_part<double, 1>(o, 0, kp.split, c0, c1);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int x0 = t + 64 * q;
+                acc[x0] = (int32_t)((uint32_t)acc[x0] + c0[q]);
+                acc[x0 + kHalf] = (int32_t)((uint32_t)acc[x0 + kHalf] + c1[q]);
+            }
+        }
+        ++k;
+        __syncthreads();  // the accumulator is updated before the next step reads it
+    }
+    if (a.acc_out) {
+        int32_t* dst = a.acc_out + (size_t)c * 2 * kN + (size_t)r * kN;
+        for (int i = threadIdx.x; i < kN; i += blockDim.x) dst[i] = acc[i];
+    }
+    if (a.lwe_out) {
+        // tLweExtractLweSample: a'_0 = a_0, a'_j = -a_{N-j} (polynomial 0),
+        // b' = b_0 (polynomial 1)
+        int32_t* dst = a.lwe_out + (size_t)c * (kN + 1);
+        if (r == 0) {
+            for (int i = threadIdx.x; i < kN; i += blockDim.x)
+                dst[i] = i == 0 ? acc[0] : (int32_t)(0u - (uint32_t)acc[kN - i]);
+        } else if (threadIdx.x == 0) {
+            dst[kN] = acc[0];
+        }
+    }
+    cluster.sync();  // no CTA leaves while its peer could still address its shared memory
+}
+
+// ----------------------------------------------------------------------
 // Blind rotation with two 64-thread halves per ciphertext (low latency).
 //
 // Half h of a ciphertext decomposes and transforms input polynomial h (rows
@@ -1821,6 +1994,19 @@ cudaError_t launch_spread2(const DevParams& P, const Tables& T, const EpArgs& a,
     return cudaGetLastError();
 }
 
+// FP64: one ciphertext per cluster of two CTAs
+template <int L>
+cudaError_t launch_spread2_f64(const DevParams& P, const Tables& T, const EpArgs& a, cudaStream_t st) {
+    if (a.count <= 0) return cudaSuccess;
+    const KParams kp = make_kparams(P);
+    using Plan = Spread2F64Plan<L>;
+    auto kern = k_blind_rotate_spread2_f64<L>;
+    cudaError_t e = set_smem(kern, Plan::request);
+    if (e != cudaSuccess) return e;
+    kern<<<2 * a.count, 64 * L, Plan::request, st>>>(kp, T, a);
+    return cudaGetLastError();
+}
+
 // split-FP32 pair kernel with `per_cta` (1..3) ciphertexts per CTA
 template <int L>
 cudaError_t launch_pair_fp32(const DevParams& P, const Tables& T, const EpArgs& a, int per_cta,
@@ -1889,7 +2075,12 @@ cudaError_t launch_ep_l(const DevParams& P, Form f, EpMode mode, const Tables& T
         case kEpPlain: return launch_ep_t<double, 1, kEpPlain, 3, L>(P, T, a, st);
         case kEpMuxRotate: return launch_ep_t<double, 1, kEpMuxRotate, 3, L>(P, T, a, st);
         default:
-            if (groups == 3) return launch_ep_t<double, 1, kEpBlindRotate, 3, L>(P, T, a, st);
+            // 0: automatic -- up to one ciphertext per two SMs on the cluster
+            // kernel, larger batches 3 per CTA with L2-direct key reads;
+            // 3: L2-direct; 4: shared key ring; 16: cluster kernel
+            if (groups == 16 || (groups == 0 && a.count <= kSmCount / 2))
+                return launch_spread2_f64<L>(P, T, a, st);
+            if (groups == 3 || groups == 0) return launch_ep_t<double, 1, kEpBlindRotate, 3, L>(P, T, a, st);
             return launch_ring_t<double, 1, 4, L, true>(P, T, a, st);
         }
     }

@@ -321,7 +321,7 @@ size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx) {
 tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,
                                             int32_t groups) {
     if (!ctx || !form_ok(form)) return TFHE_GPU_BAD_PARAM;
-    const bool ok = form == TFHE_GPU_FP64 ? (groups == 3 || groups == 4)
+    const bool ok = form == TFHE_GPU_FP64 ? (groups == 0 || groups == 3 || groups == 4 || groups == 16)
                                           : ((groups >= 0 && groups <= 16 && groups != 3));
     if (!ok) return fail(ctx, TFHE_GPU_BAD_PARAM, "unsupported groups per CTA for this form");
     ctx->groups_per_cta[form] = groups;
@@ -810,9 +810,9 @@ tfhe_gpu_status tfhe_gpu_autotune(tfhe_gpu_ctx* ctx, tfhe_gpu_form form, int32_t
     if (!form_ok(form) || count <= 0) return fail(ctx, TFHE_GPU_BAD_PARAM, "autotune args");
     RET(need_bk(ctx, form));
     static const int kFp32[] = {0, 9, 10, 6, 7, 5, 13, 12, 4, 2, 1};
-    static const int kFp64[] = {3, 4};
+    static const int kFp64[] = {0, 3, 4};
     const int* cand = form == TFHE_GPU_FP64 ? kFp64 : kFp32;
-    const int ncand = form == TFHE_GPU_FP64 ? 2 : 11;
+    const int ncand = form == TFHE_GPU_FP64 ? 3 : 11;
     const int n = ctx->P.n, nk = ctx->P.k * ctx->P.N;
     // synthetic inputs: uniform Torus32 samples (a_i = 0 would skip steps)
     std::vector<int32_t> hx((size_t)count * (n + 1));

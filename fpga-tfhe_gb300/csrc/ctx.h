@@ -30,7 +30,7 @@ struct tfhe_gpu_ctx {
     // scratch slots, grown on demand
     void* d_scratch[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t scratch_bytes[4] = {0, 0, 0, 0};
-    int groups_per_cta[kNumForms] = {3, 0};  // ciphertexts per CTA (64 threads each); 0 = automatic
+    int groups_per_cta[kNumForms] = {0, 0};  // launch shape per form; 0 = automatic
     int32_t* d_err = nullptr;  // device status word written by bounded waits (3 = timeout)
     std::string last_error;
     size_t key_bytes = 0;

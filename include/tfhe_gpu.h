@@ -130,8 +130,11 @@ size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
  *       asynchronous stores into the peer's shared memory, counted on its
  *       mbarrier (lowest latency: about 1.33 ms for a single gate's blind
  *       rotation).
- * FP64: 3 (L2) or 4 (ring, in line).  Engine tuning knob, no counterpart in
- * the reference (its kernel is a single HLS work-item). */
+ * FP64: 0 = automatic (the default): the two-SM cluster kernel for up to
+ * one ciphertext per two SMs, else 3; 3 = L2-direct key reads, 3 per CTA;
+ * 4 = shared key ring fed in line; 16 = the cluster kernel (one owner group
+ * per CTA: the FP64 key has one part).  Engine tuning knob, no counterpart
+ * in the reference (its kernel is a single HLS work-item). */
 tfhe_gpu_status tfhe_gpu_set_groups_per_cta(tfhe_gpu_ctx* ctx, tfhe_gpu_form form,
                                             int32_t groups);
 int32_t tfhe_gpu_get_groups_per_cta(const tfhe_gpu_ctx* ctx, tfhe_gpu_form form);
@@ -356,8 +359,7 @@ void tfhe_gpu_graph_destroy(tfhe_gpu_graph* graph);
 /* Time the blind-rotation launch shapes of `form` (tfhe_gpu_set_groups_per_cta)
  * on `count` synthetic ciphertexts with CUDA events, keep the fastest as the
  * context's shape and return it with its time.  The first candidate (the
- * automatic shape for split-FP32, 3 for FP64) is kept unless another shape
- * is more than 2 % faster. */
+ * automatic shape) is kept unless another shape is more than 2 % faster. */
 tfhe_gpu_status tfhe_gpu_autotune(tfhe_gpu_ctx* ctx, tfhe_gpu_form form, int32_t count,
                                   int32_t* best_shape, float* best_ms);
 

@@ -231,7 +231,7 @@ def test_errors_are_status_codes(pkg, keys, torch_cuda, P):
                                          ("split_fp32", 10), ("split_fp32", 11), ("split_fp32", 12),
                                          ("split_fp32", 13), ("split_fp32", 14),
                                          ("split_fp32", 15), ("split_fp32", 16), ("fp64", 3),
-                                         ("fp64", 4)])
+                                         ("fp64", 4), ("fp64", 0), ("fp64", 16)])
 def test_every_launch_shape(pkg, oracle, keys, torch_cuda, P, inputs, form, groups):
     """Each blind-rotation launch shape (L2-direct and shared-ring kernels) on
     a ragged batch: decrypted bits equal the truth and the oracle's, phases
@@ -607,6 +607,42 @@ def test_cluster_spread_kernel_stress_set_bit_for_bit(pkg, torch_cuda):
         e.close()
     assert (outs[14] == outs[16]).all()
     assert int((pkg.decrypt_bits(P, outs[16], lwe) != 1 - (a & b)).sum()) <= 1
+
+
+@pytest.mark.parametrize("params", ["default", "stress"])
+def test_fp64_cluster_kernel_matches_the_other_fp64_shapes(pkg, torch_cuda, params):
+    """The FP64 two-SM cluster kernel (shape 16, and the automatic shape for
+    small batches) runs the same transforms and sums the key rows in the same
+    order as the L2-direct FP64 kernel (shape 3): the ciphertexts agree bit
+    for bit, and decrypt to the truth."""
+    torch = torch_cuda
+    P = pkg.default_params() if params == "default" else pkg.stress_params()
+    lwe, tlwe, ks, bk = pkg.gate_keyset(P, [5])
+    count = 21
+    rng = np.random.default_rng(251)
+    a = rng.integers(0, 2, count)
+    b = rng.integers(0, 2, count)
+    pkg.set_seed([251])
+    d_a = torch.from_numpy(pkg.encrypt_bits(P, a, lwe)).cuda()
+    d_b = torch.from_numpy(pkg.encrypt_bits(P, b, lwe)).cuda()
+    e = pkg.Engine(P)
+    outs = {}
+    try:
+        e.upload_bootstrapping_key(bk, forms=("fp64",))
+        e.upload_keyswitch_key(ks)
+        assert e.get_groups_per_cta("fp64") == 0
+        for shape in (3, 16, 0):
+            e.set_groups_per_cta("fp64", shape)
+            d_out = torch.empty_like(d_a)
+            e.bootsGate("NAND", d_out, d_a, d_b, count, "fp64", stream=cur(torch))
+            torch.cuda.synchronize()
+            e.synchronize()
+            outs[shape] = host(d_out)
+    finally:
+        e.close()
+    assert (outs[3] == outs[16]).all()
+    assert (outs[0] == outs[16]).all()
+    assert int((pkg.decrypt_bits(P, outs[16], lwe) != 1 - (a & b)).sum()) <= (0 if params == "default" else 1)
 
 
 @pytest.mark.parametrize("count", [1000, 1])
