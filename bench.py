@@ -1158,7 +1158,7 @@ def blind_rotate_kernels(form, shape, batch, l=3):
     """Names of the blind-rotation kernels a launch of `batch` runs with
     launch shape `shape` (the engine's dispatch rules)."""
     if form == "fp64":
-        if shape == 16 or (shape == 0 and batch <= SMS // 2):
+        if shape == 16 or (shape == 0 and batch <= SMS):
             return ["k_blind_rotate_spread2_f64<%d>" % l]
         return (["k_external_product<double,1,BlindRotate,3,%d>" % l] if shape in (0, 3)
                 else ["k_blind_rotate_ring<double,1,4,%d,4,inline>" % l])

@@ -517,7 +517,7 @@ class Engine:
         14 spread kernel; 15 automatic in fixed summation order (no pair
         kernel: results independent of the batch); 16 spread kernel over a
         two-SM cluster (lowest latency).  fp64: 0 automatic (the two-SM
-        cluster kernel up to one ciphertext per two SMs, else 3); 3
+        cluster kernel up to one ciphertext per SM, else 3); 3
         L2-direct, 3 per CTA; 4 shared key ring; 16 two-SM cluster."""
         self._check(self.lib.tfhe_gpu_set_groups_per_cta(self.ctx, self._form(form), int(groups)),
                     "set_groups_per_cta")

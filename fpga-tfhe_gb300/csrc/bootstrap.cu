@@ -2075,10 +2075,12 @@ cudaError_t launch_ep_l(const DevParams& P, Form f, EpMode mode, const Tables& T
         case kEpPlain: return launch_ep_t<double, 1, kEpPlain, 3, L>(P, T, a, st);
         case kEpMuxRotate: return launch_ep_t<double, 1, kEpMuxRotate, 3, L>(P, T, a, st);
         default:
-            // 0: automatic -- up to one ciphertext per two SMs on the cluster
-            // kernel, larger batches 3 per CTA with L2-direct key reads;
-            // 3: L2-direct; 4: shared key ring; 16: cluster kernel
-            if (groups == 16 || (groups == 0 && a.count <= kSmCount / 2))
+            // 0: automatic -- up to one ciphertext per SM on the cluster
+            // kernel (one or two waves: 21.6 ms each, against about 57 ms for
+            // a wave of the 3-per-CTA kernel), larger batches 3 per CTA with
+            // L2-direct key reads; 3: L2-direct; 4: shared key ring; 16:
+            // cluster kernel
+            if (groups == 16 || (groups == 0 && a.count <= kSmCount))
                 return launch_spread2_f64<L>(P, T, a, st);
             if (groups == 3 || groups == 0) return launch_ep_t<double, 1, kEpBlindRotate, 3, L>(P, T, a, st);
             return launch_ring_t<double, 1, 4, L, true>(P, T, a, st);

@@ -131,7 +131,8 @@ size_t tfhe_gpu_device_bytes(const tfhe_gpu_ctx* ctx);
  *       mbarrier (lowest latency: about 1.33 ms for a single gate's blind
  *       rotation).
  * FP64: 0 = automatic (the default): the two-SM cluster kernel for up to
- * one ciphertext per two SMs, else 3; 3 = L2-direct key reads, 3 per CTA;
+ * one ciphertext per SM (one or two waves), else 3; 3 = L2-direct key
+ * reads, 3 per CTA;
  * 4 = shared key ring fed in line; 16 = the cluster kernel (one owner group
  * per CTA: the FP64 key has one part).  Engine tuning knob, no counterpart
  * in the reference (its kernel is a single HLS work-item). */

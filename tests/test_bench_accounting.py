@@ -58,8 +58,8 @@ def test_explicit_shapes_and_other_set():
     assert bench.blind_rotate_kernels("split_fp32", 12, 5) == [PAIR2]
     assert bench.blind_rotate_kernels("split_fp32", 10, 100, l=2) == ["k_blind_rotate_ring<float,2,6,2,4,inline,nb2>"]
     assert bench.blind_rotate_kernels("fp64", 3, 100) == ["k_external_product<double,1,BlindRotate,3,3>"]
-    assert bench.blind_rotate_kernels("fp64", 0, 100) == ["k_external_product<double,1,BlindRotate,3,3>"]
-    assert bench.blind_rotate_kernels("fp64", 0, 76) == ["k_blind_rotate_spread2_f64<3>"]
+    assert bench.blind_rotate_kernels("fp64", 0, 153) == ["k_external_product<double,1,BlindRotate,3,3>"]
+    assert bench.blind_rotate_kernels("fp64", 0, 152) == ["k_blind_rotate_spread2_f64<3>"]
     assert bench.blind_rotate_kernels("fp64", 16, 4096) == ["k_blind_rotate_spread2_f64<3>"]
 
 

@@ -609,16 +609,15 @@ def test_cluster_spread_kernel_stress_set_bit_for_bit(pkg, torch_cuda):
     assert int((pkg.decrypt_bits(P, outs[16], lwe) != 1 - (a & b)).sum()) <= 1
 
 
-@pytest.mark.parametrize("params", ["default", "stress"])
-def test_fp64_cluster_kernel_matches_the_other_fp64_shapes(pkg, torch_cuda, params):
+@pytest.mark.parametrize("params,count", [("default", 21), ("stress", 21), ("default", 150)])
+def test_fp64_cluster_kernel_matches_the_other_fp64_shapes(pkg, torch_cuda, params, count):
     """The FP64 two-SM cluster kernel (shape 16, and the automatic shape for
     small batches) runs the same transforms and sums the key rows in the same
     order as the L2-direct FP64 kernel (shape 3): the ciphertexts agree bit
-    for bit, and decrypt to the truth."""
+    for bit, and decrypt to the truth (150 gates: two waves of clusters)."""
     torch = torch_cuda
     P = pkg.default_params() if params == "default" else pkg.stress_params()
     lwe, tlwe, ks, bk = pkg.gate_keyset(P, [5])
-    count = 21
     rng = np.random.default_rng(251)
     a = rng.integers(0, 2, count)
     b = rng.integers(0, 2, count)
